@@ -1,0 +1,1879 @@
+// dompap_gpu.cu — GB300 (sm_103a) implementation of the C ABI in
+// include/dompap_gpu.h: device state, the statically compiled kernels (cell
+// list, Verlet list, integrators, reductions, layout transposes) and the NVRTC
+// pipeline that compiles the SymPy-generated pair potential together with
+// pair_kernels.cuh.
+//
+// Design (one process, one GPU, one stream per handle):
+//  * particle state lives in HBM as SoA float64 pos/vel/beta/force[k*N + i]
+//    plus int32 images; a fixed-point copy of the positions (uint32 per axis,
+//    packed in one 8/16-byte vector per particle) feeds the pair pre-filter;
+//  * the neighbour list is column-major nl[k*N + i] with counts cnt[i];
+//  * run(steps) replays CUDA graphs of `chunk` steps. Each step is
+//    [gated rebuild: cell clear, cell fill, cell sort, Verlet build, done]
+//    -> pair forces -> integrate + wrap + skin test (sets need_rebuild).
+//    The rebuild kernels return at once unless need_rebuild is set, so the
+//    graph needs no host decision. After each chunk the host reads the status
+//    word; on a neighbour-list or cell overflow it restores the chunk's start
+//    state, grows the capacity and replays the chunk.
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "dompap_gpu.h"
+#include "dp_common.cuh"
+#include "dp_embedded.h"  // dp_src_common[], dp_src_pair[] (generated at build time)
+
+// ===========================================================================
+// errors
+// ===========================================================================
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return fail(DP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define RET(call)              \
+    do {                       \
+        int rc_ = (call);      \
+        if (rc_ != DP_OK) return rc_; \
+    } while (0)
+
+static inline unsigned grid_for(long long n, int block) {
+    long long g = (n + block - 1) / block;
+    return (unsigned)std::max<long long>(1, g);
+}
+
+// ===========================================================================
+// static kernels
+// ===========================================================================
+namespace {
+
+constexpr int kBlock = 256;
+
+__global__ void k_aos_to_soa_f64(const double* __restrict__ in, double* __restrict__ out, long long n, int dim) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * dim) return;
+    const long long i = t / dim;
+    const int k = (int)(t - i * dim);
+    out[k * n + i] = in[t];
+}
+
+__global__ void k_soa_to_aos_f64(const double* __restrict__ in, double* __restrict__ out, long long n, int dim) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * dim) return;
+    const long long i = t / dim;
+    const int k = (int)(t - i * dim);
+    out[t] = in[k * n + i];
+}
+
+__global__ void k_aos_to_soa_i32(const int32_t* __restrict__ in, int32_t* __restrict__ out, long long n, int dim) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * dim) return;
+    const long long i = t / dim;
+    const int k = (int)(t - i * dim);
+    out[k * n + i] = in[t];
+}
+
+__global__ void k_soa_to_aos_i32(const int32_t* __restrict__ in, int32_t* __restrict__ out, long long n, int dim) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * dim) return;
+    const long long i = t / dim;
+    const int k = (int)(t - i * dim);
+    out[t] = in[k * n + i];
+}
+
+struct ShadowArgs {
+    const double* pos;
+    void* shadow;
+    long long n;
+    double scale[DP_MAX_DIM];
+};
+
+template <int D>
+__global__ void k_shadow(ShadowArgs a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    uint32_t u[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) u[k] = dp_fixed(a.pos[k * a.n + i], a.scale[k]);
+    ((typename dp_shadow_t<D>::type*)a.shadow)[i] = dp_shadow_pack<D>(u);
+}
+
+// --------------------------- skin test ------------------------------------
+// neighbor_list_is_old (dompap/neighbor_list.py:183-201): rebuild when some
+// particle's min-image displacement^2 since the last build exceeds (skin/2)^2.
+struct SkinArgs {
+    const double* pos;
+    const double* pos_ref;
+    dp_dev_status* st;
+    long long n;
+    double box[DP_MAX_DIM];
+    double thr;  // (0.5 * skin)^2
+};
+
+template <int D>
+__global__ void k_skin_check(SkinArgs a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool old = false;
+    if (i < a.n) {
+        double d[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) d[k] = dp_min_image(a.pos[k * a.n + i] - a.pos_ref[k * a.n + i], a.box[k]);
+        old = dp_sqsum_exact<D>(d) > a.thr;
+    }
+    if (__any_sync(0xffffffffu, old) && (threadIdx.x & 31) == 0) atomicExch(&a.st->need_rebuild, 1);
+}
+
+// --------------------------- cell list ------------------------------------
+// Cells are at least `cutoff` wide (nc = floor(L / cutoff) per axis, >= 3), so
+// every pair closer than the cutoff sits in the 3^D stencil of its cell. This
+// is the cell list of dompap/neighbor_list.py:42-180 made exact: the
+// reference uses cells of width `cutoff` with nc = ceil(L / cutoff) and misses
+// pairs when L / cutoff is not an integer.
+struct CellArgs {
+    const double* pos;
+    int32_t* cell_cnt;
+    int32_t* cell_mem;
+    dp_dev_status* st;
+    long long n;
+    long long ncell;
+    int ccap;
+    int nc[DP_MAX_DIM];
+    double inv_w[DP_MAX_DIM];
+    double box[DP_MAX_DIM];
+};
+
+// Cell of a position, binned on its periodic image in [0, L) so that positions
+// the user left outside the box are still found; the exact pair test then uses
+// the raw coordinates with the reference's single-shift rule.
+template <int D>
+__device__ __forceinline__ void cell_coords(const double* x, const int* nc, const double* inv_w, const double* box,
+                                            int* c) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        double xw = x[k];
+        if (!(xw >= 0.0 && xw < box[k])) xw -= floor(xw / box[k]) * box[k];
+        const double t = floor(xw * inv_w[k]);
+        int ck = (t >= 0.0) ? (int)fmin(t, (double)(nc[k] - 1)) : 0;  // NaN -> 0
+        c[k] = ck;
+    }
+}
+
+template <int D>
+__device__ __forceinline__ long long cell_linear(const int* c, const int* nc) {
+    long long l = c[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) l = l * nc[k] + c[k];
+    return l;
+}
+
+__global__ void k_cell_clear(CellArgs a) {
+    if (!a.st->need_rebuild) return;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < a.ncell;
+         c += (long long)gridDim.x * blockDim.x)
+        a.cell_cnt[c] = 0;
+}
+
+template <int D>
+__global__ void k_cell_fill(CellArgs a) {
+    if (!a.st->need_rebuild) return;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    double x[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) x[k] = a.pos[k * a.n + i];
+    int c[D];
+    cell_coords<D>(x, a.nc, a.inv_w, a.box, c);
+    const long long l = cell_linear<D>(c, a.nc);
+    const int slot = atomicAdd(a.cell_cnt + l, 1);
+    if (slot < a.ccap)
+        a.cell_mem[l * a.ccap + slot] = (int32_t)i;
+    else
+        atomicMax(&a.st->cell_overflow, slot + 1);
+}
+
+// Sort each cell's members by index so the Verlet rows are deterministic.
+__global__ void k_cell_sort(CellArgs a) {
+    if (!a.st->need_rebuild) return;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.ncell) return;
+    const int m = min(a.cell_cnt[c], a.ccap);
+    int32_t* mem = a.cell_mem + c * a.ccap;
+    for (int t = 1; t < m; ++t) {
+        const int32_t v = mem[t];
+        int u = t - 1;
+        while (u >= 0 && mem[u] > v) {
+            mem[u + 1] = mem[u];
+            --u;
+        }
+        mem[u + 1] = v;
+    }
+}
+
+// --------------------------- Verlet list ----------------------------------
+// get_neighbor_list_double_loop (dompap/neighbor_list.py:7-39): m is a
+// neighbour of n when sqrt(sum d^2) < cutoff with the single-shift minimum
+// image, tested in float64 without FMA (bit-identical pair set).
+struct NlArgs {
+    const double* pos;
+    double* pos_ref;
+    int32_t* nl;
+    int32_t* cnt;
+    const int32_t* cell_cnt;
+    const int32_t* cell_mem;
+    dp_dev_status* st;
+    long long n;
+    int kcap;
+    int ccap;
+    int nc[DP_MAX_DIM];
+    double inv_w[DP_MAX_DIM];
+    double box[DP_MAX_DIM];
+    double cutoff;
+};
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_nl_build_cells(NlArgs a) {
+    if (!a.st->need_rebuild) return;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const long long n = a.n;
+    double xi[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) xi[k] = a.pos[k * n + i];
+    int ci[D];
+    cell_coords<D>(xi, a.nc, a.inv_w, a.box, ci);
+    int count = 0;
+    int stencil = 1;
+#pragma unroll
+    for (int k = 0; k < D; ++k) stencil *= 3;
+    for (int s = 0; s < stencil; ++s) {
+        int cj[D];
+        int rem = s;
+#pragma unroll
+        for (int k = D - 1; k >= 0; --k) {
+            int c = ci[k] + (rem % 3) - 1;
+            rem /= 3;
+            if (c < 0) c += a.nc[k];
+            if (c >= a.nc[k]) c -= a.nc[k];
+            cj[k] = c;
+        }
+        const long long l = cell_linear<D>(cj, a.nc);
+        const int m = min(a.cell_cnt[l], a.ccap);
+        const int32_t* mem = a.cell_mem + l * a.ccap;
+        for (int t = 0; t < m; ++t) {
+            const int j = mem[t];
+            if (j == i) continue;
+            double d[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) d[k] = dp_min_image(xi[k] - a.pos[k * n + j], a.box[k]);
+            if (sqrt(dp_sqsum_exact<D>(d)) < a.cutoff) {
+                if (count < a.kcap) a.nl[(long long)count * n + i] = j;
+                ++count;
+            }
+        }
+    }
+    a.cnt[i] = min(count, a.kcap);
+    atomicMax(&a.st->max_neighbors, count);
+#pragma unroll
+    for (int k = 0; k < D; ++k) a.pos_ref[k * n + i] = xi[k];
+}
+
+// All-pairs build for boxes with fewer than 3 cells per axis; rows come out in
+// ascending index order, exactly the reference's double loop.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_nl_build_allpairs(NlArgs a) {
+    if (!a.st->need_rebuild) return;
+    __shared__ double tile[D][kBlock];
+    const long long n = a.n;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < n;
+    double xi[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) xi[k] = active ? a.pos[k * n + i] : 0.0;
+    int count = 0;
+    for (long long base = 0; base < n; base += kBlock) {
+        const long long jl = base + threadIdx.x;
+#pragma unroll
+        for (int k = 0; k < D; ++k) tile[k][threadIdx.x] = (jl < n) ? a.pos[k * n + jl] : 0.0;
+        __syncthreads();
+        if (active) {
+            const int lim = (int)min((long long)kBlock, n - base);
+            for (int t = 0; t < lim; ++t) {
+                const long long j = base + t;
+                if (j == i) continue;
+                double d[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) d[k] = dp_min_image(xi[k] - tile[k][t], a.box[k]);
+                if (sqrt(dp_sqsum_exact<D>(d)) < a.cutoff) {
+                    if (count < a.kcap) a.nl[(long long)count * n + i] = (int32_t)j;
+                    ++count;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!active) return;
+    a.cnt[i] = min(count, a.kcap);
+    atomicMax(&a.st->max_neighbors, count);
+#pragma unroll
+    for (int k = 0; k < D; ++k) a.pos_ref[k * n + i] = xi[k];
+}
+
+__global__ void k_rebuild_done(dp_dev_status* st) {
+    if (st->need_rebuild) {
+        st->need_rebuild = 0;
+        st->rebuilds += 1;
+    }
+}
+
+__global__ void k_set_rebuild(dp_dev_status* st) { st->need_rebuild = 1; }
+
+__global__ void k_advance_step(dp_dev_status* st, long long steps) { st->step += steps; }
+
+// Rows of the column-major list -> row-major (N, kout), each row sorted
+// ascending and -1 padded (dompap's neighbor_list layout).
+__global__ void k_nl_export(const int32_t* __restrict__ nl, const int32_t* __restrict__ cnt, int32_t* out,
+                            long long n, int kout) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = cnt[i];
+    int32_t* row = out + i * kout;
+    int m = 0;  // entries kept so far (<= kout), the kout smallest in ascending order
+    for (int k = 0; k < c; ++k) {
+        const int32_t v = nl[(long long)k * n + i];
+        int u;
+        if (m < kout) {
+            u = m - 1;
+            ++m;
+        } else if (v < row[kout - 1]) {
+            u = kout - 2;
+        } else {
+            continue;
+        }
+        while (u >= 0 && row[u] > v) {
+            row[u + 1] = row[u];
+            --u;
+        }
+        row[u + 1] = v;
+    }
+    for (int k = m; k < kout; ++k) row[k] = -1;
+}
+
+// --------------------------- integrators ----------------------------------
+// Mass handling: MASSMODE 0 one mass for all particles (coefficients as
+// arguments), 1 per-particle class index into a coefficient table, 2
+// per-particle masses (coefficients computed in the kernel).
+struct IntArgs {
+    double* pos;
+    double* vel;
+    double* beta;
+    const double* force;
+    int32_t* img;
+    void* shadow;
+    const double* pos_ref;
+    const uint8_t* mclass;
+    const double* mcoef;  // [class][5]: a, b*dt/m, b/(2m), sqrt(2 alpha T dt), dt/m
+    const double* mass;   // MASSMODE 2
+    dp_dev_status* st;
+    long long n;
+    double box[DP_MAX_DIM];
+    double scale[DP_MAX_DIM];
+    double thr;  // (skin/2)^2
+    double dt;
+    double coef[5];  // MASSMODE 0
+    double temperature;
+    double tau;
+    unsigned long long seed;
+    long long step_offset;
+};
+
+__device__ __forceinline__ void gjf_coefficients(double m, double dt, double T, double tau, double* c) {
+    // dompap/integrator.py:29-36
+    const double alpha = m / tau;
+    const double beta_variance = 2 * alpha * T * dt;
+    const double numerator = 1.0 - alpha * dt / 2.0 / m;
+    const double denominator = 1.0 + alpha * dt / 2.0 / m;
+    const double a = numerator / denominator;
+    const double b = 1 / denominator;
+    c[0] = a;
+    c[1] = b * dt / m;
+    c[2] = b / 2 / m;
+    c[3] = sqrt(beta_variance);
+    c[4] = dt / m;
+}
+
+template <int D, int MASSMODE>
+__device__ __forceinline__ void load_coef(const IntArgs& a, long long i, double* c) {
+    if (MASSMODE == 0) {
+#pragma unroll
+        for (int t = 0; t < 5; ++t) c[t] = a.coef[t];
+    } else if (MASSMODE == 1) {
+        const int cl = a.mclass[i];
+#pragma unroll
+        for (int t = 0; t < 5; ++t) c[t] = __ldg(a.mcoef + cl * 5 + t);
+    } else {
+        gjf_coefficients(a.mass[i], a.dt, a.temperature, a.tau, c);
+    }
+}
+
+// Wrap into [0, L) exactly as wrap_into_box (dompap/positions.py:90-98):
+// shift = floor(x / L), image += shift, x -= shift * L. For 0 <= x < L the
+// rounded x / L is < 1, so the shift is 0 and the division is skipped.
+__device__ __forceinline__ double wrap_axis(double x, double L, int32_t& image) {
+    if (!(x >= 0.0 && x < L)) {
+        const double s = floor(x / L);
+        image += (int32_t)s;
+        x -= s * L;
+    }
+    return x;
+}
+
+// Langevin G-JF leap-frog (dompap/integrator.py:17-40, arXiv:1303.7011
+// Sec. II.C eqs. 16-17), then wrap, fixed-point shadow and the skin test for
+// the next step.
+template <int D, int MASSMODE, bool NVE>
+__global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool old = false, bad = false;
+    if (i < a.n) {
+        const long long n = a.n;
+        double c[5];
+        load_coef<D, MASSMODE>(a, i, c);
+        float z[4];
+        if (!NVE) dp_normals4(a.seed, (unsigned long long)(a.st->step + a.step_offset), (uint32_t)i, z);
+        uint32_t u[D];
+        double q = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const long long o = k * n + i;
+            double v = a.vel[o];
+            double x = a.pos[o];
+            const double F = a.force[o];
+            if (NVE) {
+                v = v + c[4] * F;  // make_one_step_leap_frog (dompap/integrator.py:12)
+            } else {
+                const double bn = c[3] * (double)z[k];
+                v = c[0] * v + c[1] * F + c[2] * (a.beta[o] + bn);
+                a.beta[o] = bn;
+            }
+            x = x + v * a.dt;
+            int32_t im = a.img[o];
+            const int32_t im0 = im;
+            x = wrap_axis(x, a.box[k], im);
+            if (im != im0) a.img[o] = im;
+            a.vel[o] = v;
+            a.pos[o] = x;
+            u[k] = dp_fixed(x, a.scale[k]);
+            const double d = dp_min_image(x - a.pos_ref[o], a.box[k]);
+            q = (k == 0) ? __dmul_rn(d, d) : __dadd_rn(q, __dmul_rn(d, d));
+            bad = bad || !isfinite(x);
+        }
+        ((typename dp_shadow_t<D>::type*)a.shadow)[i] = dp_shadow_pack<D>(u);
+        old = q > a.thr;
+    }
+    const bool any_old = __any_sync(0xffffffffu, old);
+    const bool any_bad = __any_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0) {
+        if (any_old) atomicExch(&a.st->need_rebuild, 1);
+        if (any_bad) atomicExch(&a.st->nonfinite, 1);
+    }
+}
+
+// sum_n m_n |v_n|^2, per-block partials.
+template <int D, int MASSMODE>
+__global__ void __launch_bounds__(kBlock) k_sum_mv2(IntArgs a, const double* class_mass, double* partial) {
+    __shared__ double smem[32];
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < a.n) {
+        double m;
+        if (MASSMODE == 0) m = class_mass[0];
+        else if (MASSMODE == 1) m = class_mass[a.mclass[i]];
+        else m = a.mass[i];
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const double vk = a.vel[k * a.n + i];
+            s += vk * vk;
+        }
+        v = m * s;
+    }
+    v = dp_block_sum(v, smem);
+    if (threadIdx.x == 0) partial[blockIdx.x] = v;
+}
+
+// Fixed-order sum of per-block partials (one block): deterministic totals.
+__global__ void __launch_bounds__(1024) k_reduce(const double* __restrict__ partial, long long m, double* out) {
+    __shared__ double smem[32];
+    double v = 0.0;
+    for (long long t = threadIdx.x; t < m; t += blockDim.x) v += partial[t];
+    v = dp_block_sum(v, smem);
+    if (threadIdx.x == 0) out[0] = v;
+}
+
+template <int D>
+__global__ void k_normals(unsigned long long seed, long long step, double* out, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float z[4];
+    dp_normals4(seed, (unsigned long long)step, (uint32_t)i, z);
+#pragma unroll
+    for (int k = 0; k < D; ++k) out[i * D + k] = (double)z[k];
+}
+
+// wrap_into_box on demand (dompap/positions.py:90-98), with the shadow update.
+template <int D>
+__global__ void k_wrap(IntArgs a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    uint32_t u[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const long long o = k * a.n + i;
+        int32_t im = a.img[o];
+        const int32_t im0 = im;
+        const double x = wrap_axis(a.pos[o], a.box[k], im);
+        a.pos[o] = x;
+        if (im != im0) a.img[o] = im;
+        u[k] = dp_fixed(x, a.scale[k]);
+    }
+    ((typename dp_shadow_t<D>::type*)a.shadow)[i] = dp_shadow_pack<D>(u);
+}
+
+// Pair-distance histogram for g(r) (dompap/positions.py:58-87): all ordered
+// pairs (i in A, j in B, self pairs included), np.round minimum image,
+// np.histogram bins (half-open, the last one closed). The distance comes from
+// the fixed-point shadow in float32; within 1e-5 of a bin edge it is
+// recomputed in float64 exactly as NumPy does.
+struct RdfArgs {
+    const double* pos;
+    const void* shadow;
+    const int32_t* types;
+    const double* edges;
+    unsigned long long* counts;
+    long long n;
+    int nbins;
+    int type_a, type_b;  // -1: all particles
+    double box[DP_MAX_DIM];
+    float unit[DP_MAX_DIM];
+};
+
+template <int D>
+__device__ __forceinline__ int rdf_bin(double r, const double* e, int nb) {
+    if (!(r >= e[0]) || !(r <= e[nb])) return -1;
+    if (r == e[nb]) return nb - 1;
+    int lo = 0, hi = nb;  // e[lo] <= r < e[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (r >= e[mid]) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_rdf(RdfArgs a) {
+    extern __shared__ unsigned char smem_raw[];
+    double* edges = (double*)smem_raw;
+    unsigned int* hist = (unsigned int*)(edges + a.nbins + 1);
+    for (int t = threadIdx.x; t <= a.nbins; t += blockDim.x) edges[t] = a.edges[t];
+    for (int t = threadIdx.x; t < a.nbins; t += blockDim.x) hist[t] = 0u;
+    __syncthreads();
+    typedef typename dp_shadow_t<D>::type sh_t;
+    const sh_t* sh = (const sh_t*)a.shadow;
+    const long long total = a.n * a.n;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < total;
+         p += (long long)gridDim.x * blockDim.x) {
+        const long long i = p / a.n, j = p - (p / a.n) * a.n;
+        if (a.type_a >= 0 && a.types[i] != a.type_a) continue;
+        if (a.type_b >= 0 && a.types[j] != a.type_b) continue;
+        uint32_t ui[D], uj[D];
+        dp_shadow_unpack<D>(sh[i], ui);
+        dp_shadow_unpack<D>(sh[j], uj);
+        float df[D];
+        const float rf = sqrtf(dp_shadow_q<D>(ui, uj, a.unit, df));
+        int b = rdf_bin<D>((double)rf, edges, a.nbins);
+        bool near_edge = false;
+        const double tol = 1e-5 * (double)rf + 1e-9;
+        if (b >= 0) {
+            near_edge = ((double)rf - edges[b] < tol) || (edges[b + 1] - (double)rf < tol);
+        } else {
+            near_edge = fabs((double)rf - edges[0]) < tol || fabs((double)rf - edges[a.nbins]) < tol;
+        }
+        if (near_edge) {
+            double q = 0.0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                const double L = a.box[k];
+                double d = a.pos[k * a.n + i] - a.pos[k * a.n + j];
+                d -= L * rint(d / L);
+                q = (k == 0) ? __dmul_rn(d, d) : __dadd_rn(q, __dmul_rn(d, d));
+            }
+            b = rdf_bin<D>(sqrt(q), edges, a.nbins);
+        }
+        if (b >= 0) atomicAdd(hist + b, 1u);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < a.nbins; t += blockDim.x)
+        if (hist[t]) atomicAdd(a.counts + t, (unsigned long long)hist[t]);
+}
+
+}  // namespace
+
+// ===========================================================================
+// NVRTC pair-kernel libraries
+// ===========================================================================
+struct PairLib {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t forces = nullptr, energy = nullptr, virial = nullptr, laplacian = nullptr, eval = nullptr;
+};
+
+static std::mutex g_lib_mutex;
+static std::unordered_map<std::string, PairLib> g_libs;
+
+static int compile_pair_lib(const std::string& src, PairLib* out) {
+    std::lock_guard<std::mutex> lock(g_lib_mutex);
+    auto it = g_libs.find(src);
+    if (it != g_libs.end()) {
+        *out = it->second;
+        return DP_OK;
+    }
+    nvrtcProgram prog;
+    nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "dompap_pair.cu", 0, nullptr, nullptr);
+    if (r != NVRTC_SUCCESS) return fail(DP_ERR_NVRTC, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
+    const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true",
+                          "-DDP_NVRTC=1"};
+    r = nvrtcCompileProgram(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+    if (r != NVRTC_SUCCESS) {
+        size_t log_size = 0;
+        nvrtcGetProgramLogSize(prog, &log_size);
+        std::string log(log_size, '\0');
+        if (log_size) nvrtcGetProgramLog(prog, &log[0]);
+        nvrtcDestroyProgram(&prog);
+        return fail(DP_ERR_NVRTC, std::string("NVRTC compile of the pair potential failed: ") + log);
+    }
+    size_t cubin_size = 0;
+    nvrtcGetCUBINSize(prog, &cubin_size);
+    std::vector<char> cubin(cubin_size);
+    nvrtcGetCUBIN(prog, cubin.data());
+    nvrtcDestroyProgram(&prog);
+    PairLib pl;
+    CK(cudaLibraryLoadData(&pl.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+    CK(cudaLibraryGetKernel(&pl.forces, pl.lib, "dp_forces"));
+    CK(cudaLibraryGetKernel(&pl.energy, pl.lib, "dp_energy"));
+    CK(cudaLibraryGetKernel(&pl.virial, pl.lib, "dp_virial"));
+    CK(cudaLibraryGetKernel(&pl.laplacian, pl.lib, "dp_laplacian"));
+    CK(cudaLibraryGetKernel(&pl.eval, pl.lib, "dp_eval_pair"));
+    g_libs.emplace(src, pl);
+    *out = pl;
+    return DP_OK;
+}
+
+// ===========================================================================
+// handle
+// ===========================================================================
+struct GraphEntry {
+    long long steps;
+    int kind;
+    unsigned long long version;
+    cudaGraphExec_t exec;
+    long long launches;
+};
+
+struct dp_sim {
+    int dim = 3;
+    long long n = 0;
+    int precision = DP_PREC_FP64;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    double *pos = nullptr, *vel = nullptr, *beta = nullptr, *force = nullptr, *pos_ref = nullptr;
+    int32_t* img = nullptr;
+    void* shadow = nullptr;
+    size_t shadow_bytes = 0;
+    double *bk_pos = nullptr, *bk_vel = nullptr, *bk_beta = nullptr;
+    int32_t* bk_img = nullptr;
+
+    // masses
+    int mass_mode = 0;
+    std::vector<double> class_mass{1.0};
+    uint8_t* mclass = nullptr;
+    double* mcoef = nullptr;      // [nclass][5]
+    double* class_mass_dev = nullptr;
+    double* mass = nullptr;       // per particle (mode 2)
+
+    int32_t* types = nullptr;
+    bool have_types = false;
+    int min_type = 0, max_type = 0;
+    double box[DP_MAX_DIM] = {0, 0, 0, 0};
+    bool have_box = false;
+
+    // potential
+    bool have_pot = false;
+    std::string pot_src;
+    double r_cut = 1.0;
+    PairLib lib;
+    bool lib_valid = false;
+
+    // pair parameters
+    int pmode = DP_PAIR_CONST;
+    int ntypes = 1;
+    double sigma = 1.0, epsilon = 1.0, sig_max = 1.0;
+    double *sig_tab = nullptr, *eps_tab = nullptr;
+
+    // neighbour list
+    double skin = 1.0;
+    int kcap = 512;
+    int method = DP_NL_CELL;
+    bool use_cells = false;
+    double cutoff = 0.0;
+    int nc[DP_MAX_DIM] = {0, 0, 0, 0};
+    long long ncell = 0;
+    int ccap = 0;
+    int32_t *nl = nullptr, *cnt = nullptr;
+    long long nl_alloc = 0;
+    int32_t *cell_cnt = nullptr, *cell_mem = nullptr;
+    long long cell_cnt_alloc = 0, cell_mem_alloc = 0;
+    bool nl_config_dirty = true;
+    bool nl_built = false;
+
+    // integrator
+    double dt = 0.01, temperature = 1.0, tau = 0.1;
+    unsigned long long seed = 0;
+
+    dp_dev_status* dstat = nullptr;
+    dp_dev_status* hstat = nullptr;  // pinned
+    double* partial = nullptr;
+    long long partial_alloc = 0;
+    double* dsum = nullptr;
+    double* hsum = nullptr;  // pinned
+
+    unsigned long long version = 1;
+    std::vector<GraphEntry> graphs;
+    long long launches_last = 0;
+};
+
+// ---------------------------------------------------------------------------
+static void free_graphs(dp_sim* s) {
+    for (auto& g : s->graphs) cudaGraphExecDestroy(g.exec);
+    s->graphs.clear();
+}
+
+static int dalloc(void** p, size_t bytes) {
+    if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    if (bytes == 0) return DP_OK;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(DP_ERR_CUDA, std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+    }
+    return DP_OK;
+}
+
+template <typename T>
+static int dalloc_t(T** p, size_t count) {
+    return dalloc((void**)p, count * sizeof(T));
+}
+
+static int ensure_partial(dp_sim* s, long long blocks) {
+    if (blocks <= s->partial_alloc) return DP_OK;
+    RET(dalloc_t(&s->partial, (size_t)blocks));
+    s->partial_alloc = blocks;
+    s->version++;
+    return DP_OK;
+}
+
+static void fill_scale(const dp_sim* s, double* scale, float* unit) {
+    for (int k = 0; k < DP_MAX_DIM; ++k) {
+        const double L = (k < s->dim) ? s->box[k] : 1.0;
+        if (scale) scale[k] = 4294967296.0 / L;
+        if (unit) unit[k] = (float)(L / 4294967296.0);
+    }
+}
+
+static int launch_shadow(dp_sim* s) {
+    ShadowArgs a{};
+    a.pos = s->pos;
+    a.shadow = s->shadow;
+    a.n = s->n;
+    fill_scale(s, a.scale, nullptr);
+    const unsigned g = grid_for(s->n, kBlock);
+    switch (s->dim) {
+        case 2: k_shadow<2><<<g, kBlock, 0, s->stream>>>(a); break;
+        case 3: k_shadow<3><<<g, kBlock, 0, s->stream>>>(a); break;
+        default: k_shadow<4><<<g, kBlock, 0, s->stream>>>(a); break;
+    }
+    CK(cudaGetLastError());
+    return DP_OK;
+}
+
+// --------------------------- mass classes ---------------------------------
+static int upload_mass_coefficients(dp_sim* s) {
+    const int nclass = (int)s->class_mass.size();
+    std::vector<double> coef((size_t)nclass * 5);
+    for (int c = 0; c < nclass; ++c) {
+        const double m = s->class_mass[c];
+        const double alpha = m / s->tau;
+        const double beta_variance = 2 * alpha * s->temperature * s->dt;
+        const double numerator = 1.0 - alpha * s->dt / 2.0 / m;
+        const double denominator = 1.0 + alpha * s->dt / 2.0 / m;
+        const double a = numerator / denominator;
+        const double b = 1 / denominator;
+        coef[c * 5 + 0] = a;
+        coef[c * 5 + 1] = b * s->dt / m;
+        coef[c * 5 + 2] = b / 2 / m;
+        coef[c * 5 + 3] = std::sqrt(beta_variance);
+        coef[c * 5 + 4] = s->dt / m;
+    }
+    RET(dalloc_t(&s->mcoef, coef.size()));
+    CK(cudaMemcpy(s->mcoef, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice));
+    RET(dalloc_t(&s->class_mass_dev, (size_t)nclass));
+    CK(cudaMemcpy(s->class_mass_dev, s->class_mass.data(), nclass * sizeof(double), cudaMemcpyHostToDevice));
+    s->version++;
+    return DP_OK;
+}
+
+// --------------------------- neighbour-list configuration -----------------
+static int configure_nl(dp_sim* s) {
+    if (!s->nl_config_dirty) return DP_OK;
+    if (!s->have_box) return fail(DP_ERR_ARG, "box not set");
+    const double reach = s->sig_max * s->r_cut;
+    s->cutoff = reach + s->skin;  // dompap/Simulation.py:353-356
+    bool cells = s->method == DP_NL_CELL && std::isfinite(s->cutoff) && s->cutoff > 0;
+    long long ncell = 1;
+    for (int k = 0; k < s->dim && cells; ++k) {
+        // a relative margin keeps every cell strictly wider than the cutoff
+        const double w = s->cutoff * (1.0 + 1e-10);
+        const double ncd = std::floor(s->box[k] / w);
+        if (!(ncd >= 3.0) || ncd > 1e6) {
+            cells = false;
+            break;
+        }
+        s->nc[k] = (int)ncd;
+        ncell *= s->nc[k];
+        if (ncell > (1LL << 31)) cells = false;
+    }
+    s->use_cells = cells;
+    if (!cells) {
+        for (int k = 0; k < DP_MAX_DIM; ++k) s->nc[k] = 0;
+        s->ncell = 0;
+    } else {
+        for (int k = s->dim; k < DP_MAX_DIM; ++k) s->nc[k] = 1;
+        s->ncell = ncell;
+        const double avg = (double)s->n / (double)ncell;
+        int cap = (int)std::ceil(avg * 2.0 + 8.0);
+        cap = (cap + 3) & ~3;
+        s->ccap = std::max(s->ccap, cap);
+        if (s->ncell > s->cell_cnt_alloc) {
+            RET(dalloc_t(&s->cell_cnt, (size_t)s->ncell));
+            s->cell_cnt_alloc = s->ncell;
+        }
+        if (s->ncell * s->ccap > s->cell_mem_alloc) {
+            RET(dalloc_t(&s->cell_mem, (size_t)(s->ncell * s->ccap)));
+            s->cell_mem_alloc = s->ncell * s->ccap;
+        }
+    }
+    const long long need = (long long)s->kcap * s->n;
+    if (need > s->nl_alloc) {
+        RET(dalloc_t(&s->nl, (size_t)need));
+        s->nl_alloc = need;
+    }
+    s->nl_config_dirty = false;
+    s->nl_built = false;
+    s->version++;
+    return DP_OK;
+}
+
+static void fill_cell_args(const dp_sim* s, CellArgs& a) {
+    a.pos = s->pos;
+    a.cell_cnt = s->cell_cnt;
+    a.cell_mem = s->cell_mem;
+    a.st = s->dstat;
+    a.n = s->n;
+    a.ncell = s->ncell;
+    a.ccap = s->ccap;
+    for (int k = 0; k < DP_MAX_DIM; ++k) {
+        a.nc[k] = s->nc[k];
+        a.inv_w[k] = (k < s->dim && s->nc[k] > 0) ? (double)s->nc[k] / s->box[k] : 0.0;
+        a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
+    }
+}
+
+// The gated rebuild sequence (no effect unless need_rebuild is set).
+static int launch_rebuild(dp_sim* s, long long* launches) {
+    const unsigned gp = grid_for(s->n, kBlock);
+    NlArgs na{};
+    na.pos = s->pos;
+    na.pos_ref = s->pos_ref;
+    na.nl = s->nl;
+    na.cnt = s->cnt;
+    na.cell_cnt = s->cell_cnt;
+    na.cell_mem = s->cell_mem;
+    na.st = s->dstat;
+    na.n = s->n;
+    na.kcap = s->kcap;
+    na.ccap = s->ccap;
+    na.cutoff = s->cutoff;
+    for (int k = 0; k < DP_MAX_DIM; ++k) na.box[k] = (k < s->dim) ? s->box[k] : 1.0;
+    long long nl_launches = 0;
+    if (s->use_cells) {
+        CellArgs ca{};
+        fill_cell_args(s, ca);
+        for (int k = 0; k < DP_MAX_DIM; ++k) {
+            na.nc[k] = ca.nc[k];
+            na.inv_w[k] = ca.inv_w[k];
+        }
+        const unsigned gc = (unsigned)std::min<long long>(grid_for(s->ncell, kBlock), 4096);
+        k_cell_clear<<<gc, kBlock, 0, s->stream>>>(ca);
+        switch (s->dim) {
+            case 2: k_cell_fill<2><<<gp, kBlock, 0, s->stream>>>(ca); break;
+            case 3: k_cell_fill<3><<<gp, kBlock, 0, s->stream>>>(ca); break;
+            default: k_cell_fill<4><<<gp, kBlock, 0, s->stream>>>(ca); break;
+        }
+        k_cell_sort<<<grid_for(s->ncell, kBlock), kBlock, 0, s->stream>>>(ca);
+        switch (s->dim) {
+            case 2: k_nl_build_cells<2><<<gp, kBlock, 0, s->stream>>>(na); break;
+            case 3: k_nl_build_cells<3><<<gp, kBlock, 0, s->stream>>>(na); break;
+            default: k_nl_build_cells<4><<<gp, kBlock, 0, s->stream>>>(na); break;
+        }
+        nl_launches = 4;
+    } else {
+        switch (s->dim) {
+            case 2: k_nl_build_allpairs<2><<<gp, kBlock, 0, s->stream>>>(na); break;
+            case 3: k_nl_build_allpairs<3><<<gp, kBlock, 0, s->stream>>>(na); break;
+            default: k_nl_build_allpairs<4><<<gp, kBlock, 0, s->stream>>>(na); break;
+        }
+        nl_launches = 1;
+    }
+    k_rebuild_done<<<1, 1, 0, s->stream>>>(s->dstat);
+    CK(cudaGetLastError());
+    if (launches) *launches += nl_launches + 1;
+    return DP_OK;
+}
+
+static void fill_pair_args(const dp_sim* s, dp_pair_args& a, double* out) {
+    memset(&a, 0, sizeof(a));
+    a.pos = s->pos;
+    a.shadow = s->shadow;
+    a.nl = s->nl;
+    a.cnt = s->cnt;
+    a.types = s->types;
+    a.sig_tab = s->sig_tab;
+    a.eps_tab = s->eps_tab;
+    a.out = out;
+    a.partial = s->partial;
+    a.status = s->dstat;
+    a.n = s->n;
+    a.ntypes = s->ntypes;
+    for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
+    fill_scale(s, nullptr, a.unit);
+    a.sigma = s->sigma;
+    a.epsilon = s->epsilon;
+    a.rcut = s->r_cut;
+    // Pre-filter threshold: a pair is skipped only when its float32 distance,
+    // whose error is < 1e-6 relative plus a few L / 2^32, certainly exceeds
+    // r_cut * sigma_max.
+    double lmax = 0.0;
+    for (int k = 0; k < s->dim; ++k) lmax = std::max(lmax, s->box[k]);
+    const double reach = s->r_cut * s->sig_max;
+    if (std::isfinite(reach)) {
+        const double rr = reach * (1.0 + 1e-5) + 8.0 * lmax / 4294967296.0 * std::sqrt((double)s->dim) + 1e-30;
+        a.cut2f = (float)(rr * rr * (1.0 + 1e-6));
+    } else {
+        a.cut2f = INFINITY;
+    }
+}
+
+static int launch_pair(dp_sim* s, cudaKernel_t k, double* out, long long* launches) {
+    dp_pair_args a;
+    fill_pair_args(s, a, out);
+    void* args[] = {&a};
+    CK(cudaLaunchKernel((const void*)k, dim3(grid_for(s->n, kBlock)), dim3(kBlock), args, 0, s->stream));
+    if (launches) *launches += 1;
+    return DP_OK;
+}
+
+static void fill_int_args(const dp_sim* s, IntArgs& a, long long step_offset) {
+    memset(&a, 0, sizeof(a));
+    a.pos = s->pos;
+    a.vel = s->vel;
+    a.beta = s->beta;
+    a.force = s->force;
+    a.img = s->img;
+    a.shadow = s->shadow;
+    a.pos_ref = s->pos_ref;
+    a.mclass = s->mclass;
+    a.mcoef = s->mcoef;
+    a.mass = s->mass;
+    a.st = s->dstat;
+    a.n = s->n;
+    for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
+    fill_scale(s, a.scale, nullptr);
+    a.thr = (0.5 * s->skin) * (0.5 * s->skin);
+    a.dt = s->dt;
+    {
+        const double m = s->class_mass[0];
+        const double alpha = m / s->tau;
+        const double beta_variance = 2 * alpha * s->temperature * s->dt;
+        const double numerator = 1.0 - alpha * s->dt / 2.0 / m;
+        const double denominator = 1.0 + alpha * s->dt / 2.0 / m;
+        const double aa = numerator / denominator;
+        const double b = 1 / denominator;
+        a.coef[0] = aa;
+        a.coef[1] = b * s->dt / m;
+        a.coef[2] = b / 2 / m;
+        a.coef[3] = std::sqrt(beta_variance);
+        a.coef[4] = s->dt / m;
+    }
+    a.temperature = s->temperature;
+    a.tau = s->tau;
+    a.seed = s->seed;
+    a.step_offset = step_offset;
+}
+
+template <int D, bool NVE>
+static void launch_integrate_d(dp_sim* s, const IntArgs& a) {
+    const unsigned g = grid_for(s->n, kBlock);
+    switch (s->mass_mode) {
+        case 0: k_integrate<D, 0, NVE><<<g, kBlock, 0, s->stream>>>(a); break;
+        case 1: k_integrate<D, 1, NVE><<<g, kBlock, 0, s->stream>>>(a); break;
+        default: k_integrate<D, 2, NVE><<<g, kBlock, 0, s->stream>>>(a); break;
+    }
+}
+
+static int launch_integrate(dp_sim* s, int kind, long long step_offset, long long* launches) {
+    IntArgs a;
+    fill_int_args(s, a, step_offset);
+    const bool nve = kind == DP_INT_NVE;
+    switch (s->dim) {
+        case 2: nve ? launch_integrate_d<2, true>(s, a) : launch_integrate_d<2, false>(s, a); break;
+        case 3: nve ? launch_integrate_d<3, true>(s, a) : launch_integrate_d<3, false>(s, a); break;
+        default: nve ? launch_integrate_d<4, true>(s, a) : launch_integrate_d<4, false>(s, a); break;
+    }
+    CK(cudaGetLastError());
+    if (launches) *launches += 1;
+    return DP_OK;
+}
+
+static int launch_skin_check(dp_sim* s) {
+    SkinArgs a{};
+    a.pos = s->pos;
+    a.pos_ref = s->pos_ref;
+    a.st = s->dstat;
+    a.n = s->n;
+    for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
+    a.thr = (0.5 * s->skin) * (0.5 * s->skin);
+    const unsigned g = grid_for(s->n, kBlock);
+    switch (s->dim) {
+        case 2: k_skin_check<2><<<g, kBlock, 0, s->stream>>>(a); break;
+        case 3: k_skin_check<3><<<g, kBlock, 0, s->stream>>>(a); break;
+        default: k_skin_check<4><<<g, kBlock, 0, s->stream>>>(a); break;
+    }
+    CK(cudaGetLastError());
+    return DP_OK;
+}
+
+static int read_status(dp_sim* s) {
+    CK(cudaMemcpyAsync(s->hstat, s->dstat, sizeof(dp_dev_status), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return DP_OK;
+}
+
+static int write_status(dp_sim* s) {
+    CK(cudaMemcpyAsync(s->dstat, s->hstat, sizeof(dp_dev_status), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return DP_OK;
+}
+
+static int require_ready(dp_sim* s) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    if (!s->have_box) return fail(DP_ERR_ARG, "box not set");
+    if (!s->have_pot || !s->lib_valid) return fail(DP_ERR_NOPOT, "no pair potential set");
+    return DP_OK;
+}
+
+// Grow capacities after an overflow reported in hstat; returns 1 if grown.
+static int grow_after_overflow(dp_sim* s, bool* grown) {
+    *grown = false;
+    if (s->hstat->cell_overflow > 0 && s->use_cells) {
+        s->ccap = ((int)(s->hstat->cell_overflow * 1.5) + 8 + 3) & ~3;
+        if (s->ncell * s->ccap > s->cell_mem_alloc) {
+            RET(dalloc_t(&s->cell_mem, (size_t)(s->ncell * s->ccap)));
+            s->cell_mem_alloc = s->ncell * s->ccap;
+        }
+        s->hstat->cell_overflow = 0;
+        *grown = true;
+    }
+    if (s->hstat->max_neighbors > s->kcap) {
+        const int want = ((int)(s->hstat->max_neighbors * 1.25) + 32 + 31) & ~31;
+        s->kcap = want;
+        const long long need = (long long)s->kcap * s->n;
+        if (need > s->nl_alloc) {
+            RET(dalloc_t(&s->nl, (size_t)need));
+            s->nl_alloc = need;
+        }
+        *grown = true;
+    }
+    if (*grown) {
+        s->version++;
+        s->hstat->max_neighbors = 0;
+    }
+    return DP_OK;
+}
+
+// Rebuild now if needed (check) or unconditionally; handles overflow growth.
+static int update_nl(dp_sim* s, bool check, int* rebuilt) {
+    RET(configure_nl(s));
+    RET(read_status(s));
+    const long long before = s->hstat->rebuilds;
+    if (!s->nl_built || !check) {
+        s->hstat->need_rebuild = 1;
+        RET(write_status(s));
+    } else {
+        RET(launch_skin_check(s));
+    }
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        RET(read_status(s));
+        const bool was_needed = s->hstat->need_rebuild != 0;
+        if (!was_needed) break;
+        s->hstat->max_neighbors = 0;
+        s->hstat->cell_overflow = 0;
+        RET(write_status(s));
+        RET(launch_rebuild(s, nullptr));
+        RET(read_status(s));
+        bool grown = false;
+        RET(grow_after_overflow(s, &grown));
+        if (!grown) break;
+        s->hstat->need_rebuild = 1;
+        RET(write_status(s));
+    }
+    s->nl_built = true;
+    if (rebuilt) *rebuilt = (s->hstat->rebuilds != before) ? 1 : 0;
+    return DP_OK;
+}
+
+// --------------------------- graphs ---------------------------------------
+static int record_steps(dp_sim* s, long long steps, int kind, long long* launches) {
+    for (long long t = 0; t < steps; ++t) {
+        RET(launch_rebuild(s, launches));
+        RET(launch_pair(s, s->lib.forces, s->force, launches));
+        RET(launch_integrate(s, kind, t, launches));
+    }
+    k_advance_step<<<1, 1, 0, s->stream>>>(s->dstat, steps);
+    CK(cudaGetLastError());
+    *launches += 1;
+    return DP_OK;
+}
+
+static int get_graph(dp_sim* s, long long steps, int kind, GraphEntry** out) {
+    for (auto& g : s->graphs) {
+        if (g.steps == steps && g.kind == kind && g.version == s->version) {
+            *out = &g;
+            return DP_OK;
+        }
+    }
+    // drop stale graphs
+    for (auto it = s->graphs.begin(); it != s->graphs.end();) {
+        if (it->version != s->version) {
+            cudaGraphExecDestroy(it->exec);
+            it = s->graphs.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    long long launches = 0;
+    const int rc = record_steps(s, steps, kind, &launches);
+    cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+    if (rc != DP_OK) return rc;
+    if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    GraphEntry g;
+    g.steps = steps;
+    g.kind = kind;
+    g.version = s->version;
+    g.launches = launches;
+    e = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    s->graphs.push_back(g);
+    *out = &s->graphs.back();
+    return DP_OK;
+}
+
+static int backup_state(dp_sim* s) {
+    const size_t bd = (size_t)s->n * s->dim * sizeof(double);
+    const size_t bi = (size_t)s->n * s->dim * sizeof(int32_t);
+    CK(cudaMemcpyAsync(s->bk_pos, s->pos, bd, cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->bk_vel, s->vel, bd, cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->bk_beta, s->beta, bd, cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->bk_img, s->img, bi, cudaMemcpyDeviceToDevice, s->stream));
+    return DP_OK;
+}
+
+static int restore_state(dp_sim* s) {
+    const size_t bd = (size_t)s->n * s->dim * sizeof(double);
+    const size_t bi = (size_t)s->n * s->dim * sizeof(int32_t);
+    CK(cudaMemcpyAsync(s->pos, s->bk_pos, bd, cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->vel, s->bk_vel, bd, cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->beta, s->bk_beta, bd, cudaMemcpyDeviceToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->img, s->bk_img, bi, cudaMemcpyDeviceToDevice, s->stream));
+    return launch_shadow(s);
+}
+
+static long long chunk_steps(const dp_sim* s) {
+    long long c = (4LL << 20) / std::max<long long>(1, s->n);
+    c = std::max<long long>(32, std::min<long long>(1024, c));
+    return c;
+}
+
+static int run_impl(dp_sim* s, long long steps, int kind, float* ms) {
+    RET(require_ready(s));
+    if (kind != DP_INT_GJF && kind != DP_INT_NVE) return fail(DP_ERR_ARG, "unknown integrator kind");
+    if (steps < 0) return fail(DP_ERR_ARG, "steps must be >= 0");
+    // make the list current (the reference checks it at the start of every step)
+    RET(update_nl(s, true, nullptr));
+    RET(ensure_partial(s, grid_for(s->n, kBlock)));
+    s->launches_last = 0;
+    if (ms) CK(cudaEventRecord(s->ev0, s->stream));
+    const long long chunk = chunk_steps(s);
+    long long done = 0;
+    int retries = 0;
+    while (done < steps) {
+        const long long c = std::min(chunk, steps - done);
+        const long long step0 = s->hstat->step;  // hstat is current: every path here ends in read_status
+        RET(backup_state(s));
+        GraphEntry* g = nullptr;
+        RET(get_graph(s, c, kind, &g));
+        CK(cudaGraphLaunch(g->exec, s->stream));
+        RET(read_status(s));
+        if (s->hstat->nonfinite) {
+            s->hstat->nonfinite = 0;
+            RET(write_status(s));
+            return fail(DP_ERR_NONFINITE, "a force or position became NaN/Inf during run()");
+        }
+        bool grown = false;
+        RET(grow_after_overflow(s, &grown));
+        if (grown) {
+            if (++retries > 8) return fail(DP_ERR_OVERFLOW, "neighbour list keeps overflowing");
+            RET(restore_state(s));
+            s->hstat->step = step0;
+            s->hstat->need_rebuild = 1;
+            RET(write_status(s));
+            continue;  // replay the chunk with the larger capacity
+        }
+        s->launches_last += g->launches;
+        done += c;
+    }
+    if (ms) {
+        CK(cudaEventRecord(s->ev1, s->stream));
+        CK(cudaEventSynchronize(s->ev1));
+        CK(cudaEventElapsedTime(ms, s->ev0, s->ev1));
+    }
+    return DP_OK;
+}
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* dp_last_error(void) { return g_err.c_str(); }
+
+int dp_version(void) { return 100; }
+
+int dp_create(int dim, int64_t n, int precision, dp_sim** out) {
+    if (!out) return fail(DP_ERR_ARG, "out is null");
+    *out = nullptr;
+    if (dim < 2 || dim > 4) return fail(DP_ERR_ARG, "dimension must be 2, 3 or 4");
+    if (n < 1 || n > 2147483647LL) return fail(DP_ERR_ARG, "number of particles must be in [1, 2^31)");
+    if (precision != DP_PREC_FP64 && precision != DP_PREC_FP32) return fail(DP_ERR_ARG, "unknown precision");
+    dp_sim* s = new dp_sim();
+    s->dim = dim;
+    s->n = n;
+    s->precision = precision;
+    int rc = DP_OK;
+    auto cleanup = [&]() {
+        dp_destroy(s);
+        return rc;
+    };
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess) {
+        rc = fail(DP_ERR_CUDA, std::string("stream/event creation: ") + cudaGetErrorString(cudaGetLastError()));
+        return cleanup();
+    }
+    const size_t nd = (size_t)n * dim;
+    if ((rc = dalloc_t(&s->pos, nd)) || (rc = dalloc_t(&s->vel, nd)) || (rc = dalloc_t(&s->beta, nd)) ||
+        (rc = dalloc_t(&s->force, nd)) || (rc = dalloc_t(&s->pos_ref, nd)) || (rc = dalloc_t(&s->img, nd)) ||
+        (rc = dalloc_t(&s->bk_pos, nd)) || (rc = dalloc_t(&s->bk_vel, nd)) || (rc = dalloc_t(&s->bk_beta, nd)) ||
+        (rc = dalloc_t(&s->bk_img, nd)) || (rc = dalloc_t(&s->cnt, (size_t)n)))
+        return cleanup();
+    s->shadow_bytes = (size_t)n * (dim == 2 ? 8 : 16);
+    if ((rc = dalloc(&s->shadow, s->shadow_bytes))) return cleanup();
+    if (cudaMemset(s->pos, 0, nd * 8) != cudaSuccess || cudaMemset(s->vel, 0, nd * 8) != cudaSuccess ||
+        cudaMemset(s->beta, 0, nd * 8) != cudaSuccess || cudaMemset(s->force, 0, nd * 8) != cudaSuccess ||
+        cudaMemset(s->pos_ref, 0, nd * 8) != cudaSuccess || cudaMemset(s->img, 0, nd * 4) != cudaSuccess ||
+        cudaMemset(s->cnt, 0, (size_t)n * 4) != cudaSuccess) {
+        rc = fail(DP_ERR_CUDA, "cudaMemset failed");
+        return cleanup();
+    }
+    if (cudaMalloc(&s->dstat, sizeof(dp_dev_status)) != cudaSuccess ||
+        cudaMallocHost(&s->hstat, sizeof(dp_dev_status)) != cudaSuccess ||
+        cudaMalloc(&s->dsum, sizeof(double)) != cudaSuccess || cudaMallocHost(&s->hsum, sizeof(double)) != cudaSuccess) {
+        rc = fail(DP_ERR_CUDA, "status allocation failed");
+        return cleanup();
+    }
+    memset(s->hstat, 0, sizeof(dp_dev_status));
+    if (cudaMemcpy(s->dstat, s->hstat, sizeof(dp_dev_status), cudaMemcpyHostToDevice) != cudaSuccess) {
+        rc = fail(DP_ERR_CUDA, "status init failed");
+        return cleanup();
+    }
+    if ((rc = upload_mass_coefficients(s))) return cleanup();
+    *out = s;
+    return DP_OK;
+}
+
+int dp_destroy(dp_sim* s) {
+    if (!s) return DP_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    free_graphs(s);
+    void* bufs[] = {s->pos, s->vel, s->beta, s->force, s->pos_ref, s->img, s->shadow, s->bk_pos, s->bk_vel,
+                    s->bk_beta, s->bk_img, s->mclass, s->mcoef, s->class_mass_dev, s->mass, s->types, s->sig_tab,
+                    s->eps_tab, s->nl, s->cnt, s->cell_cnt, s->cell_mem, s->dstat, s->partial, s->dsum};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    if (s->hstat) cudaFreeHost(s->hstat);
+    if (s->hsum) cudaFreeHost(s->hsum);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return DP_OK;
+}
+
+static int rebuild_pair_lib(dp_sim* s);
+
+int dp_set_precision(dp_sim* s, int precision) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    if (precision != DP_PREC_FP64 && precision != DP_PREC_FP32) return fail(DP_ERR_ARG, "unknown precision");
+    if (precision == s->precision) return DP_OK;
+    s->precision = precision;
+    if (s->have_pot) RET(rebuild_pair_lib(s));
+    return DP_OK;
+}
+
+// --------------------------- state ----------------------------------------
+static int upload_aos_f64(dp_sim* s, const double* host, double* dev_soa) {
+    if (!host) return fail(DP_ERR_ARG, "null array");
+    const size_t bytes = (size_t)s->n * s->dim * sizeof(double);
+    // stage through the force buffer's twin (bk_pos) to transpose on the device
+    CK(cudaMemcpyAsync(s->bk_pos, host, bytes, cudaMemcpyHostToDevice, s->stream));
+    k_aos_to_soa_f64<<<grid_for(s->n * s->dim, kBlock), kBlock, 0, s->stream>>>(s->bk_pos, dev_soa, s->n, s->dim);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    return DP_OK;
+}
+
+static int download_aos_f64(dp_sim* s, const double* dev_soa, double* host) {
+    if (!host) return fail(DP_ERR_ARG, "null array");
+    const size_t bytes = (size_t)s->n * s->dim * sizeof(double);
+    k_soa_to_aos_f64<<<grid_for(s->n * s->dim, kBlock), kBlock, 0, s->stream>>>(dev_soa, s->bk_vel, s->n, s->dim);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host, s->bk_vel, bytes, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return DP_OK;
+}
+
+int dp_set_positions(dp_sim* s, const double* p) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    RET(upload_aos_f64(s, p, s->pos));
+    if (s->have_box) RET(launch_shadow(s));
+    CK(cudaStreamSynchronize(s->stream));
+    return DP_OK;
+}
+int dp_get_positions(dp_sim* s, double* p) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    return download_aos_f64(s, s->pos, p);
+}
+int dp_get_reference_positions(dp_sim* s, double* p) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    return download_aos_f64(s, s->pos_ref, p);
+}
+int dp_set_velocities(dp_sim* s, const double* v) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    return upload_aos_f64(s, v, s->vel);
+}
+int dp_get_velocities(dp_sim* s, double* v) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    return download_aos_f64(s, s->vel, v);
+}
+int dp_set_betas(dp_sim* s, const double* b) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    return upload_aos_f64(s, b, s->beta);
+}
+int dp_get_betas(dp_sim* s, double* b) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    return download_aos_f64(s, s->beta, b);
+}
+int dp_set_images(dp_sim* s, const int32_t* im) {
+    if (!s || !im) return fail(DP_ERR_ARG, "null argument");
+    const size_t bytes = (size_t)s->n * s->dim * sizeof(int32_t);
+    CK(cudaMemcpyAsync(s->bk_img, im, bytes, cudaMemcpyHostToDevice, s->stream));
+    k_aos_to_soa_i32<<<grid_for(s->n * s->dim, kBlock), kBlock, 0, s->stream>>>(s->bk_img, s->img, s->n, s->dim);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    return DP_OK;
+}
+int dp_get_images(dp_sim* s, int32_t* im) {
+    if (!s || !im) return fail(DP_ERR_ARG, "null argument");
+    const size_t bytes = (size_t)s->n * s->dim * sizeof(int32_t);
+    k_soa_to_aos_i32<<<grid_for(s->n * s->dim, kBlock), kBlock, 0, s->stream>>>(s->img, s->bk_img, s->n, s->dim);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(im, s->bk_img, bytes, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return DP_OK;
+}
+
+int dp_set_masses(dp_sim* s, const double* m) {
+    if (!s || !m) return fail(DP_ERR_ARG, "null argument");
+    std::map<double, int> classes;
+    for (long long i = 0; i < s->n && classes.size() <= 256; ++i) classes.emplace(m[i], 0);
+    if (classes.size() == 1) {
+        s->mass_mode = 0;
+        s->class_mass.assign(1, m[0]);
+    } else if (classes.size() <= 256) {
+        s->mass_mode = 1;
+        s->class_mass.clear();
+        int c = 0;
+        for (auto& kv : classes) {
+            kv.second = c++;
+            s->class_mass.push_back(kv.first);
+        }
+        std::vector<uint8_t> cls((size_t)s->n);
+        for (long long i = 0; i < s->n; ++i) cls[i] = (uint8_t)classes[m[i]];
+        RET(dalloc_t(&s->mclass, (size_t)s->n));
+        CK(cudaMemcpy(s->mclass, cls.data(), (size_t)s->n, cudaMemcpyHostToDevice));
+    } else {
+        s->mass_mode = 2;
+        s->class_mass.assign(1, m[0]);
+        RET(dalloc_t(&s->mass, (size_t)s->n));
+        CK(cudaMemcpy(s->mass, m, (size_t)s->n * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    if (s->mass_mode == 2) {
+        // the reduction kernels read per-particle masses
+        RET(dalloc_t(&s->class_mass_dev, 1));
+        CK(cudaMemcpy(s->class_mass_dev, s->class_mass.data(), sizeof(double), cudaMemcpyHostToDevice));
+    }
+    return upload_mass_coefficients(s);
+}
+
+int dp_set_types(dp_sim* s, const int32_t* t) {
+    if (!s || !t) return fail(DP_ERR_ARG, "null argument");
+    int lo = t[0], hi = t[0];
+    for (long long i = 1; i < s->n; ++i) {
+        lo = std::min(lo, (int)t[i]);
+        hi = std::max(hi, (int)t[i]);
+    }
+    if (lo < 0) return fail(DP_ERR_ARG, "particle types must be >= 0");
+    if (s->pmode == DP_PAIR_TYPES && hi >= s->ntypes)
+        return fail(DP_ERR_ARG, "a particle type exceeds the per-type parameter table");
+    s->min_type = lo;
+    s->max_type = hi;
+    if (!s->types) RET(dalloc_t(&s->types, (size_t)s->n));
+    CK(cudaMemcpy(s->types, t, (size_t)s->n * sizeof(int32_t), cudaMemcpyHostToDevice));
+    s->have_types = true;
+    s->version++;
+    return DP_OK;
+}
+
+int dp_set_box(dp_sim* s, const double* box) {
+    if (!s || !box) return fail(DP_ERR_ARG, "null argument");
+    for (int k = 0; k < s->dim; ++k) {
+        if (!(box[k] > 0.0) || !std::isfinite(box[k])) return fail(DP_ERR_ARG, "box sides must be positive and finite");
+        s->box[k] = box[k];
+    }
+    s->have_box = true;
+    s->nl_config_dirty = true;
+    s->version++;
+    return launch_shadow(s);
+}
+
+// --------------------------- potential ------------------------------------
+static std::string hexd(double v) {
+    if (std::isinf(v)) return v > 0 ? "(1.0/0.0)" : "(-1.0/0.0)";
+    char buf[64];
+    snprintf(buf, sizeof(buf), "%a", v);
+    return buf;
+}
+
+static int rebuild_pair_lib(dp_sim* s) {
+    std::string src;
+    src += "#define DP_DIM " + std::to_string(s->dim) + "\n";
+    if (s->precision == DP_PREC_FP32) {
+        src += "#define DP_REAL float\n#define DP_REAL_IS_FLOAT 1\n";
+    } else {
+        src += "#define DP_REAL double\n#define DP_REAL_IS_FLOAT 0\n";
+    }
+    src += "#define DP_PMODE " + std::to_string(s->pmode) + "\n";
+    const bool sig_one = s->pmode == DP_PAIR_CONST && s->sigma == 1.0;
+    const bool eps_one = s->pmode == DP_PAIR_CONST && s->epsilon == 1.0;
+    src += std::string("#define DP_SIGMA_ONE ") + (sig_one ? "1" : "0") + "\n";
+    src += std::string("#define DP_EPS_ONE ") + (eps_one ? "1" : "0") + "\n";
+    src += dp_src_common;
+    src += "\n// ---- generated pair potential ----\n";
+    src += s->pot_src;
+    src += "\n// ---- pair kernels ----\n";
+    src += dp_src_pair;
+    PairLib pl;
+    RET(compile_pair_lib(src, &pl));
+    s->lib = pl;
+    s->lib_valid = true;
+    s->version++;
+    return DP_OK;
+}
+
+int dp_set_potential(dp_sim* s, const char* device_source, double r_cut) {
+    if (!s || !device_source) return fail(DP_ERR_ARG, "null argument");
+    if (!(r_cut > 0.0)) return fail(DP_ERR_ARG, "r_cut must be positive");
+    s->pot_src = device_source;
+    s->r_cut = r_cut;
+    s->have_pot = true;
+    s->lib_valid = false;
+    RET(rebuild_pair_lib(s));
+    s->nl_config_dirty = true;
+    return DP_OK;
+}
+
+int dp_set_pair_params(dp_sim* s, int mode, int ntypes, const double* sigma, const double* epsilon) {
+    if (!s || !sigma || !epsilon) return fail(DP_ERR_ARG, "null argument");
+    double smax = 0.0;
+    if (mode == DP_PAIR_CONST) {
+        s->sigma = sigma[0];
+        s->epsilon = epsilon[0];
+        smax = sigma[0];
+        s->ntypes = 1;
+    } else if (mode == DP_PAIR_TYPES) {
+        if (ntypes < 1 || ntypes > 4096) return fail(DP_ERR_ARG, "ntypes must be in [1, 4096]");
+        if (!s->have_types) return fail(DP_ERR_ARG, "per-type parameters need particle types (dp_set_types)");
+        if (s->max_type >= ntypes) return fail(DP_ERR_ARG, "a particle type exceeds the per-type parameter table");
+        const size_t m = (size_t)ntypes * ntypes;
+        for (size_t t = 0; t < m; ++t) smax = std::max(smax, sigma[t]);
+        RET(dalloc_t(&s->sig_tab, m));
+        RET(dalloc_t(&s->eps_tab, m));
+        CK(cudaMemcpy(s->sig_tab, sigma, m * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(s->eps_tab, epsilon, m * sizeof(double), cudaMemcpyHostToDevice));
+        s->ntypes = ntypes;
+    } else if (mode == DP_PAIR_DENSE) {
+        const size_t m = (size_t)s->n * s->n;
+        for (size_t t = 0; t < m; ++t) smax = std::max(smax, sigma[t]);
+        RET(dalloc_t(&s->sig_tab, m));
+        RET(dalloc_t(&s->eps_tab, m));
+        CK(cudaMemcpy(s->sig_tab, sigma, m * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(s->eps_tab, epsilon, m * sizeof(double), cudaMemcpyHostToDevice));
+        s->ntypes = 1;
+    } else {
+        return fail(DP_ERR_ARG, "unknown pair-parameter mode");
+    }
+    if (!(smax > 0.0)) return fail(DP_ERR_ARG, "the largest sigma must be positive");
+    s->pmode = mode;
+    s->sig_max = smax;  // largest sigma (dompap/Simulation.py:346-351)
+    s->nl_config_dirty = true;
+    s->version++;
+    if (s->have_pot) RET(rebuild_pair_lib(s));
+    return DP_OK;
+}
+
+int dp_set_neighbor_list(dp_sim* s, double skin, int max_neighbors, int method) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    if (!(skin >= 0.0)) return fail(DP_ERR_ARG, "skin must be >= 0");
+    if (max_neighbors < 1) return fail(DP_ERR_ARG, "max_number_of_neighbors must be >= 1");
+    if (method != DP_NL_CELL && method != DP_NL_ALLPAIRS) return fail(DP_ERR_ARG, "unknown neighbour-list method");
+    s->skin = skin;
+    s->kcap = max_neighbors;
+    s->method = method;
+    s->nl_config_dirty = true;
+    s->version++;
+    return DP_OK;
+}
+
+int dp_update_neighbor_list(dp_sim* s, int check, int* rebuilt) {
+    RET(require_ready(s));
+    return update_nl(s, check != 0, rebuilt);
+}
+
+int dp_get_neighbor_list(dp_sim* s, int32_t* out, int kmax, int32_t* max_count) {
+    RET(require_ready(s));
+    if (!out || kmax < 1) return fail(DP_ERR_ARG, "bad output");
+    RET(update_nl(s, true, nullptr));
+    int32_t* dout = nullptr;
+    RET(dalloc_t(&dout, (size_t)s->n * kmax));
+    k_nl_export<<<grid_for(s->n, kBlock), kBlock, 0, s->stream>>>(s->nl, s->cnt, dout, s->n, kmax);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, dout, (size_t)s->n * kmax * sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(dout);
+    if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("neighbour-list export: ") + cudaGetErrorString(e));
+    if (max_count) *max_count = s->hstat->max_neighbors;
+    return DP_OK;
+}
+
+int dp_set_integrator(dp_sim* s, double time_step, double temperature, double damping_time, uint64_t seed) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    s->dt = time_step;
+    s->temperature = temperature;
+    s->tau = damping_time;
+    s->seed = seed;
+    s->version++;
+    return upload_mass_coefficients(s);
+}
+
+int dp_run(dp_sim* s, int64_t steps, int kind) { return run_impl(s, steps, kind, nullptr); }
+
+int dp_run_timed(dp_sim* s, int64_t steps, int kind, float* ms) {
+    if (!ms) return fail(DP_ERR_ARG, "ms is null");
+    return run_impl(s, steps, kind, ms);
+}
+
+// --------------------------- observables ----------------------------------
+int dp_forces(dp_sim* s, double* forces) {
+    RET(require_ready(s));
+    RET(update_nl(s, true, nullptr));
+    RET(launch_pair(s, s->lib.forces, s->force, nullptr));
+    RET(read_status(s));
+    if (s->hstat->nonfinite) {
+        s->hstat->nonfinite = 0;
+        RET(write_status(s));
+    }
+    return download_aos_f64(s, s->force, forces);
+}
+
+static int scalar_pair(dp_sim* s, cudaKernel_t k, double* out) {
+    RET(require_ready(s));
+    if (!out) return fail(DP_ERR_ARG, "null output");
+    RET(update_nl(s, true, nullptr));
+    const long long blocks = grid_for(s->n, kBlock);
+    RET(ensure_partial(s, blocks));
+    RET(launch_pair(s, k, nullptr, nullptr));
+    k_reduce<<<1, 1024, 0, s->stream>>>(s->partial, blocks, s->dsum);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(s->hsum, s->dsum, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    *out = *s->hsum;
+    return DP_OK;
+}
+
+int dp_potential_energy(dp_sim* s, double* energy) {
+    double e = 0.0;
+    RET(scalar_pair(s, s ? s->lib.energy : nullptr, &e));
+    *energy = e / 2;
+    return DP_OK;
+}
+
+int dp_virial(dp_sim* s, double* virial) {
+    double w = 0.0;
+    RET(scalar_pair(s, s ? s->lib.virial : nullptr, &w));
+    *virial = w / 2 / s->dim;
+    return DP_OK;
+}
+
+int dp_laplacian(dp_sim* s, double* lap) {
+    RET(require_ready(s));
+    if (!lap) return fail(DP_ERR_ARG, "null output");
+    RET(update_nl(s, true, nullptr));
+    RET(launch_pair(s, s->lib.laplacian, s->bk_beta, nullptr));
+    CK(cudaMemcpyAsync(lap, s->bk_beta, (size_t)s->n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return DP_OK;
+}
+
+int dp_sum_mv2(dp_sim* s, double* out) {
+    if (!s || !out) return fail(DP_ERR_ARG, "null argument");
+    const long long blocks = grid_for(s->n, kBlock);
+    RET(ensure_partial(s, blocks));
+    IntArgs a;
+    fill_int_args(s, a, 0);
+    const unsigned g = (unsigned)blocks;
+#define DP_MV2(D)                                                                                               \
+    switch (s->mass_mode) {                                                                                     \
+        case 0: k_sum_mv2<D, 0><<<g, kBlock, 0, s->stream>>>(a, s->class_mass_dev, s->partial); break;          \
+        case 1: k_sum_mv2<D, 1><<<g, kBlock, 0, s->stream>>>(a, s->class_mass_dev, s->partial); break;          \
+        default: k_sum_mv2<D, 2><<<g, kBlock, 0, s->stream>>>(a, s->class_mass_dev, s->partial); break;         \
+    }
+    switch (s->dim) {
+        case 2: DP_MV2(2); break;
+        case 3: DP_MV2(3); break;
+        default: DP_MV2(4); break;
+    }
+#undef DP_MV2
+    k_reduce<<<1, 1024, 0, s->stream>>>(s->partial, blocks, s->dsum);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(s->hsum, s->dsum, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    *out = *s->hsum;
+    return DP_OK;
+}
+
+int dp_eval_potential(dp_sim* s, const double* sv, int64_t n, double* u, double* f, double* c) {
+    if (!s || !sv || !u || !f || !c) return fail(DP_ERR_ARG, "null argument");
+    if (!s->have_pot || !s->lib_valid) return fail(DP_ERR_NOPOT, "no pair potential set");
+    if (n <= 0) return DP_OK;
+    double* buf = nullptr;
+    RET(dalloc_t(&buf, (size_t)n * 4));
+    const size_t b = (size_t)n * sizeof(double);
+    cudaError_t e = cudaMemcpyAsync(buf, sv, b, cudaMemcpyHostToDevice, s->stream);
+    double* du = buf + n;
+    double* df = buf + 2 * n;
+    double* dc = buf + 3 * n;
+    long long nn = n;
+    double rc = s->r_cut;
+    void* args[] = {&buf, &du, &df, &dc, &nn, &rc};
+    if (e == cudaSuccess)
+        e = cudaLaunchKernel((const void*)s->lib.eval, dim3(grid_for(n, kBlock)), dim3(kBlock), args, 0, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(u, du, b, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(f, df, b, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c, dc, b, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("dp_eval_potential: ") + cudaGetErrorString(e));
+    return DP_OK;
+}
+
+int dp_get_normals(dp_sim* s, int64_t step, double* out) {
+    if (!s || !out) return fail(DP_ERR_ARG, "null argument");
+    const unsigned g = grid_for(s->n, kBlock);
+    switch (s->dim) {
+        case 2: k_normals<2><<<g, kBlock, 0, s->stream>>>(s->seed, step, s->bk_vel, s->n); break;
+        case 3: k_normals<3><<<g, kBlock, 0, s->stream>>>(s->seed, step, s->bk_vel, s->n); break;
+        default: k_normals<4><<<g, kBlock, 0, s->stream>>>(s->seed, step, s->bk_vel, s->n); break;
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, s->bk_vel, (size_t)s->n * s->dim * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return DP_OK;
+}
+
+int dp_get_stats(dp_sim* s, dp_stats* st) {
+    if (!s || !st) return fail(DP_ERR_ARG, "null argument");
+    RET(read_status(s));
+    memset(st, 0, sizeof(*st));
+    st->steps = s->hstat->step;
+    st->rebuilds = s->hstat->rebuilds;
+    st->max_neighbors = s->hstat->max_neighbors;
+    st->neighbor_capacity = s->kcap;
+    for (int k = 0; k < 4; ++k) st->cells[k] = s->use_cells ? s->nc[k] : 0;
+    st->cell_capacity = s->ccap;
+    st->method_used = s->use_cells ? DP_NL_CELL : DP_NL_ALLPAIRS;
+    st->nl_cutoff = s->cutoff;
+    return DP_OK;
+}
+
+int dp_time_forces(dp_sim* s, int reps, float* ms) {
+    RET(require_ready(s));
+    if (!ms || reps < 1) return fail(DP_ERR_ARG, "bad arguments");
+    RET(update_nl(s, true, nullptr));
+    RET(launch_pair(s, s->lib.forces, s->force, nullptr));  // warm-up
+    CK(cudaEventRecord(s->ev0, s->stream));
+    for (int r = 0; r < reps; ++r) RET(launch_pair(s, s->lib.forces, s->force, nullptr));
+    CK(cudaEventRecord(s->ev1, s->stream));
+    CK(cudaEventSynchronize(s->ev1));
+    float t = 0.0f;
+    CK(cudaEventElapsedTime(&t, s->ev0, s->ev1));
+    *ms = t / reps;
+    return DP_OK;
+}
+
+int dp_wrap(dp_sim* s) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    if (!s->have_box) return fail(DP_ERR_ARG, "box not set");
+    IntArgs a;
+    fill_int_args(s, a, 0);
+    const unsigned g = grid_for(s->n, kBlock);
+    switch (s->dim) {
+        case 2: k_wrap<2><<<g, kBlock, 0, s->stream>>>(a); break;
+        case 3: k_wrap<3><<<g, kBlock, 0, s->stream>>>(a); break;
+        default: k_wrap<4><<<g, kBlock, 0, s->stream>>>(a); break;
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    return DP_OK;
+}
+
+int dp_rdf_counts(dp_sim* s, int type_a, int type_b, const double* edges, int nbins, uint64_t* counts) {
+    if (!s || !edges || !counts) return fail(DP_ERR_ARG, "null argument");
+    if (!s->have_box) return fail(DP_ERR_ARG, "box not set");
+    if (nbins < 1 || nbins > 8192) return fail(DP_ERR_ARG, "nbins must be in [1, 8192]");
+    if ((type_a >= 0 || type_b >= 0) && !s->have_types) return fail(DP_ERR_ARG, "particle types not set");
+    for (int b = 0; b < nbins; ++b)
+        if (!(edges[b] <= edges[b + 1])) return fail(DP_ERR_ARG, "r_bins array must be sorted in ascending order.");
+    double* dedges = nullptr;
+    unsigned long long* dcounts = nullptr;
+    RET(dalloc_t(&dedges, (size_t)nbins + 1));
+    int rc = dalloc_t(&dcounts, (size_t)nbins);
+    if (rc) {
+        cudaFree(dedges);
+        return rc;
+    }
+    RdfArgs a{};
+    a.pos = s->pos;
+    a.shadow = s->shadow;
+    a.types = s->types;
+    a.edges = dedges;
+    a.counts = dcounts;
+    a.n = s->n;
+    a.nbins = nbins;
+    a.type_a = type_a;
+    a.type_b = type_b;
+    for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
+    fill_scale(s, nullptr, a.unit);
+    const size_t smem = (size_t)(nbins + 1) * sizeof(double) + (size_t)nbins * sizeof(unsigned int);
+    const long long pairs = s->n * s->n;
+    const unsigned g = (unsigned)std::min<long long>(grid_for(pairs, kBlock), 152LL * 8);
+    cudaError_t e = cudaMemcpyAsync(dedges, edges, (nbins + 1) * sizeof(double), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dcounts, 0, nbins * sizeof(unsigned long long), s->stream);
+    if (e == cudaSuccess && smem > 48 * 1024) {
+        switch (s->dim) {
+            case 2: e = cudaFuncSetAttribute(k_rdf<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); break;
+            case 3: e = cudaFuncSetAttribute(k_rdf<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); break;
+            default: e = cudaFuncSetAttribute(k_rdf<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); break;
+        }
+    }
+    if (e == cudaSuccess) {
+        switch (s->dim) {
+            case 2: k_rdf<2><<<g, kBlock, smem, s->stream>>>(a); break;
+            case 3: k_rdf<3><<<g, kBlock, smem, s->stream>>>(a); break;
+            default: k_rdf<4><<<g, kBlock, smem, s->stream>>>(a); break;
+        }
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(counts, dcounts, nbins * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(dedges);
+    cudaFree(dcounts);
+    if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("dp_rdf_counts: ") + cudaGetErrorString(e));
+    return DP_OK;
+}
+
+int64_t dp_kernel_launches(dp_sim* s) { return s ? s->launches_last : 0; }
+
+}  // extern "C"

@@ -1,0 +1,209 @@
+// dp_common.cuh — device helpers shared by the statically compiled kernels
+// (dompap_gpu.cu) and the NVRTC-compiled pair kernels (pair_kernels.cuh).
+//
+// Everything here is plain CUDA C++ with no includes, so that the same text is
+// compiled by nvcc and embedded verbatim into NVRTC programs.
+#pragma once
+
+#ifdef __CUDACC_RTC__
+typedef int int32_t;
+typedef unsigned int uint32_t;
+typedef long long int64_t;
+typedef unsigned long long uint64_t;
+typedef unsigned char uint8_t;
+#endif
+
+#define DP_MAX_DIM 4
+
+// Device status word shared by every kernel of one simulation handle. The host
+// reads it (pinned mirror) after each chunk of steps.
+struct dp_dev_status {
+    int32_t need_rebuild;     // 1: the next step rebuilds the neighbour list
+    int32_t max_neighbors;    // largest neighbour count seen by the last build
+    int32_t cell_overflow;    // largest cell occupancy seen when it exceeded capacity
+    int32_t nonfinite;        // a force or position became NaN/Inf
+    int64_t rebuilds;         // neighbour-list builds done on the device
+    int64_t step;             // steps integrated (the RNG counter)
+};
+
+// Arguments of the NVRTC-compiled pair kernels (pair_kernels.cuh); the host
+// fills the same struct, so the layout is shared by construction.
+struct dp_pair_args {
+    const double* pos;
+    const void* shadow;
+    const int32_t* nl;
+    const int32_t* cnt;
+    const int32_t* types;
+    const double* sig_tab;
+    const double* eps_tab;
+    double* out;
+    double* partial;
+    dp_dev_status* status;
+    long long n;
+    int ntypes;
+    int pad0;
+    double box[DP_MAX_DIM];
+    float unit[DP_MAX_DIM];  // L / 2^32 per axis
+    double sigma;            // DP_PMODE == 0
+    double epsilon;          // DP_PMODE == 0
+    double rcut;             // r_cut in units of sigma
+    float cut2f;             // pre-filter: skip a pair when its float32 r^2 exceeds this
+    int pad1;
+};
+
+// ---------------------------------------------------------------------------
+// Minimum image, single +-L shift per axis, exactly as
+// dompap/positions.py:12-16 (box/2 is exact in binary floating point).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dp_min_image(double d, double L) {
+    const double half = 0.5 * L;
+    if (d > half) {
+        d -= L;
+    } else if (d < -half) {
+        d += L;
+    }
+    return d;
+}
+
+// Sequential d0^2 + d1^2 + ... without FMA contraction, matching the order and
+// rounding of NumPy/Numba summing a short float64 vector (bit-exact pair test,
+// dompap/neighbor_list.py:32-33).
+template <int D>
+__device__ __forceinline__ double dp_sqsum_exact(const double* d) {
+    double q = __dmul_rn(d[0], d[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) q = __dadd_rn(q, __dmul_rn(d[k], d[k]));
+    return q;
+}
+
+// ---------------------------------------------------------------------------
+// Fixed-point position shadow: u = floor(x * 2^32 / L) mod 2^32 per axis.
+// The wrap-around difference (int32)(u_i - u_j) is the nearest-image
+// displacement in units of L / 2^32, so the pair pre-filter needs no float64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t dp_fixed(double x, double scale /* 2^32 / L */) {
+    const long long t = __double2ll_rd(x * scale);
+    return (uint32_t)(unsigned long long)t;
+}
+
+template <int D>
+struct dp_shadow_t;
+template <>
+struct dp_shadow_t<2> {
+    typedef uint2 type;
+};
+template <>
+struct dp_shadow_t<3> {
+    typedef uint4 type;
+};
+template <>
+struct dp_shadow_t<4> {
+    typedef uint4 type;
+};
+
+template <int D>
+__device__ __forceinline__ void dp_shadow_unpack(const typename dp_shadow_t<D>::type& s, uint32_t* u);
+template <>
+__device__ __forceinline__ void dp_shadow_unpack<2>(const uint2& s, uint32_t* u) {
+    u[0] = s.x;
+    u[1] = s.y;
+}
+template <>
+__device__ __forceinline__ void dp_shadow_unpack<3>(const uint4& s, uint32_t* u) {
+    u[0] = s.x;
+    u[1] = s.y;
+    u[2] = s.z;
+}
+template <>
+__device__ __forceinline__ void dp_shadow_unpack<4>(const uint4& s, uint32_t* u) {
+    u[0] = s.x;
+    u[1] = s.y;
+    u[2] = s.z;
+    u[3] = s.w;
+}
+
+template <int D>
+__device__ __forceinline__ typename dp_shadow_t<D>::type dp_shadow_pack(const uint32_t* u);
+template <>
+__device__ __forceinline__ uint2 dp_shadow_pack<2>(const uint32_t* u) {
+    return make_uint2(u[0], u[1]);
+}
+template <>
+__device__ __forceinline__ uint4 dp_shadow_pack<3>(const uint32_t* u) {
+    return make_uint4(u[0], u[1], u[2], 0u);
+}
+template <>
+__device__ __forceinline__ uint4 dp_shadow_pack<4>(const uint32_t* u) {
+    return make_uint4(u[0], u[1], u[2], u[3]);
+}
+
+// Float32 squared displacement from two fixed-point shadows.
+template <int D>
+__device__ __forceinline__ float dp_shadow_q(const uint32_t* ui, const uint32_t* uj, const float* unit,
+                                             float* df) {
+    float q = 0.0f;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const int n = (int)(ui[k] - uj[k]);
+        df[k] = (float)n * unit[k];
+        q = fmaf(df[k], df[k], q);
+    }
+    return q;
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, SC'11),
+// written from the published round function and constants.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 dp_philox4x32_10(uint4 ctr, uint2 key) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int round = 0; round < 10; ++round) {
+        const uint32_t hi0 = __umulhi(M0, ctr.x), lo0 = M0 * ctr.x;
+        const uint32_t hi1 = __umulhi(M1, ctr.z), lo1 = M1 * ctr.z;
+        ctr = make_uint4(hi1 ^ ctr.y ^ key.x, lo1, hi0 ^ ctr.w ^ key.y, lo0);
+        key.x += W0;
+        key.y += W1;
+    }
+    return ctr;
+}
+
+// Four standard normal deviates for (particle, step) by the Box-Muller
+// transform of two Philox outputs pairs.
+__device__ __forceinline__ void dp_normals4(uint64_t seed, uint64_t step, uint32_t particle, float* z) {
+    const uint4 r = dp_philox4x32_10(make_uint4(particle, (uint32_t)step, (uint32_t)(step >> 32), 0x64706d64u),
+                                     make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+    const float two_pow_m32 = 2.3283064365386963e-10f;
+    // u in (0, 1] for the logarithm, v in [0, 1) for the angle
+    const float u0 = ((float)r.x + 1.0f) * two_pow_m32;
+    const float v0 = (float)r.y * two_pow_m32;
+    const float u1 = ((float)r.z + 1.0f) * two_pow_m32;
+    const float v1 = (float)r.w * two_pow_m32;
+    const float rad0 = sqrtf(-2.0f * logf(fminf(u0, 1.0f)));
+    const float rad1 = sqrtf(-2.0f * logf(fminf(u1, 1.0f)));
+    float s0, c0, s1, c1;
+    sincospif(2.0f * v0, &s0, &c0);
+    sincospif(2.0f * v1, &s1, &c1);
+    z[0] = rad0 * c0;
+    z[1] = rad0 * s0;
+    z[2] = rad1 * c1;
+    z[3] = rad1 * s1;
+}
+
+// Block-wide float64 sum (blockDim.x a multiple of 32, <= 1024); result valid
+// in thread 0. Uses warp shuffles, then one warp over the per-warp sums.
+__device__ __forceinline__ double dp_block_sum(double v, double* smem /* >= 32 doubles */) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) smem[warp] = v;
+    __syncthreads();
+    const int nwarps = (blockDim.x + 31) >> 5;
+    v = (threadIdx.x < nwarps) ? smem[threadIdx.x] : 0.0;
+    if (warp == 0) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    return v;
+}

@@ -1,0 +1,209 @@
+// pair_kernels.cuh — pair force / energy / virial / Laplacian kernels.
+//
+// This file is compiled at run time by NVRTC for sm_103a, once per
+// (dimension, pair potential, sigma/epsilon mode, precision). The host
+// prepends the DP_* configuration macros, dp_common.cuh and the device
+// functions generated from the SymPy pair potential:
+//
+//   template <typename R> __device__ R dp_pair_u(R s);   // u(s) - u(r_cut)
+//   template <typename R> __device__ R dp_pair_f(R s);   // -du/ds
+//   template <typename R> __device__ R dp_pair_c(R s);   // d2u/ds2
+//
+// Semantics follow dompap's neighbour-list kernels:
+//   force      dompap/potential.py:163-188  F_n = sum_m eps f(r/sigma) d/r
+//   energy     dompap/potential.py:69-100   U = 1/2 sum_n sum_m eps u(r/sigma)
+//   virial     dompap/potential.py:253-279  W = 1/D sum_{n<m} eps f(r/sigma) r
+//   laplacian  dompap/potential.py:327-364  sum_m eps c(r/sigma) - (D-1) eps f(r/sigma)/r
+// with s = r / sigma and every term 0 where s > r_cut (dompap/potential.py:61-65).
+// There is no 1/sigma chain-rule factor, exactly as in the reference.
+//
+// Layout in HBM: positions are SoA float64 pos[k*N + i]; the neighbour list
+// is column-major nl[k*N + i] with per-particle counts cnt[i]; the
+// fixed-point shadow is one 8- or 16-byte vector per particle.
+//
+// Configuration macros (set by the host):
+//   DP_DIM          spatial dimension (2, 3 or 4)
+//   DP_REAL         pair arithmetic type: double (FP64 mode) or float (FP32 mode)
+//   DP_PMODE        0 constant sigma/epsilon, 1 per-type table, 2 dense (N, N) matrix
+//   DP_SIGMA_ONE    1 when sigma is the constant 1 (the division is skipped)
+//   DP_EPS_ONE      1 when epsilon is the constant 1
+
+#ifndef DP_DIM
+#error "DP_DIM must be defined"
+#endif
+
+// struct dp_pair_args is defined in dp_common.cuh (shared with the host).
+
+typedef DP_REAL real_t;
+typedef typename dp_shadow_t<DP_DIM>::type shadow_t;
+
+__device__ __forceinline__ void dp_pair_params(const dp_pair_args& a, long long i, int ti, int j, double& sig,
+                                               double& eps) {
+#if DP_PMODE == 0
+    sig = a.sigma;
+    eps = a.epsilon;
+#elif DP_PMODE == 1
+    const int tj = __ldg(a.types + j);
+    sig = __ldg(a.sig_tab + ti * a.ntypes + tj);
+    eps = __ldg(a.eps_tab + ti * a.ntypes + tj);
+#else
+    sig = __ldg(a.sig_tab + i * a.n + j);
+    eps = __ldg(a.eps_tab + i * a.n + j);
+#endif
+}
+
+// What one kernel accumulates for a pair; selected at compile time.
+enum { DP_ACC_FORCE = 0, DP_ACC_ENERGY = 1, DP_ACC_VIRIAL = 2, DP_ACC_LAPLACE = 3 };
+
+// Per-particle neighbour loop. Returns the scalar sum (energy / virial /
+// Laplacian) and, for DP_ACC_FORCE, the force vector in f[].
+template <int ACC>
+__device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long long i, double* f) {
+    constexpr int D = DP_DIM;
+    const long long n = a.n;
+    const shadow_t* __restrict__ sh = (const shadow_t*)a.shadow;
+    uint32_t ui[D];
+    dp_shadow_unpack<D>(sh[i], ui);
+    double xi[D];
+#if !(DP_REAL_IS_FLOAT)
+#pragma unroll
+    for (int k = 0; k < D; ++k) xi[k] = a.pos[k * n + i];
+#endif
+    int ti = 0;
+#if DP_PMODE == 1
+    ti = a.types[i];
+#endif
+    real_t acc_v[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) acc_v[k] = real_t(0);
+    double acc_s = 0.0;
+    const int c = a.cnt[i];
+    const int32_t* __restrict__ row = a.nl + i;
+    for (int kk = 0; kk < c; ++kk) {
+        const int j = __ldg(row + (long long)kk * n);
+        uint32_t uj[D];
+        dp_shadow_unpack<D>(__ldg(sh + j), uj);
+        float df[D];
+        const float qf = dp_shadow_q<D>(ui, uj, a.unit, df);
+        if (qf > a.cut2f) continue;  // certainly beyond r_cut * sigma_max
+        double sig, eps;
+        dp_pair_params(a, i, ti, j, sig, eps);
+#if DP_REAL_IS_FLOAT
+        // FP32 pair arithmetic on the fixed-point displacement.
+        const float r = sqrtf(qf);
+#if DP_SIGMA_ONE
+        const float s = r;
+#else
+        const float s = r / (float)sig;
+#endif
+        if (s > (float)a.rcut) continue;
+        const float e = (float)eps;
+        if (ACC == DP_ACC_FORCE) {
+#if DP_EPS_ONE
+            const float sf = dp_pair_f<float>(s);
+#else
+            const float sf = e * dp_pair_f<float>(s);
+#endif
+            const float g = sf / r;
+#pragma unroll
+            for (int k = 0; k < D; ++k) acc_v[k] = fmaf(g, df[k], acc_v[k]);
+        } else if (ACC == DP_ACC_ENERGY) {
+            acc_s += (double)(e * dp_pair_u<float>(s));
+        } else if (ACC == DP_ACC_VIRIAL) {
+            acc_s += (double)(e * dp_pair_f<float>(s) * r);
+        } else {
+            acc_s += (double)(e * dp_pair_c<float>(s) + (float)(D - 1) * (-e * dp_pair_f<float>(s)) / r);
+        }
+#else
+        // FP64 pair arithmetic, reference order of operations.
+        double d[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) d[k] = dp_min_image(xi[k] - __ldg(a.pos + k * n + j), a.box[k]);
+        const double q = dp_sqsum_exact<D>(d);
+        const double r = sqrt(q);
+#if DP_SIGMA_ONE
+        const double s = r;
+#else
+        const double s = r / sig;
+#endif
+        if (s > a.rcut) continue;
+        if (ACC == DP_ACC_FORCE) {
+#if DP_EPS_ONE
+            const double sf = dp_pair_f<double>(s);
+#else
+            const double sf = eps * dp_pair_f<double>(s);
+#endif
+#pragma unroll
+            for (int k = 0; k < D; ++k) acc_v[k] += sf * (d[k] / r);
+        } else if (ACC == DP_ACC_ENERGY) {
+            acc_s += eps * dp_pair_u<double>(s);
+        } else if (ACC == DP_ACC_VIRIAL) {
+            acc_s += eps * dp_pair_f<double>(s) * r;
+        } else {
+            const double sf = eps * dp_pair_f<double>(s);
+            acc_s += eps * dp_pair_c<double>(s) + (double)(D - 1) * (-sf) / r;
+        }
+#endif
+    }
+    if (ACC == DP_ACC_FORCE) {
+#pragma unroll
+        for (int k = 0; k < D; ++k) f[k] = (double)acc_v[k];
+    }
+    return acc_s;
+}
+
+// F (SoA float64) for every particle. One thread per particle.
+extern "C" __global__ void __launch_bounds__(256) dp_forces(dp_pair_args a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    double f[DP_DIM];
+    dp_particle_sum<DP_ACC_FORCE>(a, i, f);
+    bool finite = true;
+#pragma unroll
+    for (int k = 0; k < DP_DIM; ++k) {
+        a.out[k * a.n + i] = f[k];
+        finite = finite && isfinite(f[k]);
+    }
+    if (!finite) atomicExch(&a.status->nonfinite, 1);
+}
+
+// Per-block partial sums of a scalar pair quantity (energy or virial); the
+// host-side reduction kernel adds the partials in a fixed order.
+template <int ACC>
+__device__ __forceinline__ void dp_scalar_partial(const dp_pair_args& a) {
+    __shared__ double smem[32];
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < a.n) v = dp_particle_sum<ACC>(a, i, nullptr);
+    v = dp_block_sum(v, smem);
+    if (threadIdx.x == 0) a.partial[blockIdx.x] = v;
+}
+
+extern "C" __global__ void __launch_bounds__(256) dp_energy(dp_pair_args a) { dp_scalar_partial<DP_ACC_ENERGY>(a); }
+
+extern "C" __global__ void __launch_bounds__(256) dp_virial(dp_pair_args a) { dp_scalar_partial<DP_ACC_VIRIAL>(a); }
+
+// Per-particle Laplacian of the potential energy (float64 out[i]).
+extern "C" __global__ void __launch_bounds__(256) dp_laplacian(dp_pair_args a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    a.out[i] = dp_particle_sum<DP_ACC_LAPLACE>(a, i, nullptr);
+}
+
+// u_cut, f_cut, c_cut of the compiled potential at scaled distances s[i]
+// (the reference's pair_potential / pair_force / pair_curvature callables).
+extern "C" __global__ void dp_eval_pair(const double* s_in, double* u, double* f, double* c, long long n,
+                                        double rcut) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double s = s_in[i];
+    if (s > rcut) {
+        u[i] = 0.0;
+        f[i] = 0.0;
+        c[i] = 0.0;
+        return;
+    }
+    u[i] = (double)dp_pair_u<real_t>((real_t)s);
+    f[i] = (double)dp_pair_f<real_t>((real_t)s);
+    c[i] = (double)dp_pair_c<real_t>((real_t)s);
+}

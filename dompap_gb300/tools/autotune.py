@@ -1,0 +1,72 @@
+"""GPU autotuner with the interface of dompap/tools/autotune.py:4-178.
+
+Same procedure as dompap's: time the two neighbour-list build methods (best of
+4 forced rebuilds), then scan the skin upward from ``smallest_skin`` in steps
+of ``step_skin`` while the time of ``steps`` steps keeps falling (up to half
+the smallest box side), and keep the fastest setting. Timings of runs are
+device times (CUDA events on the system's stream); builds are timed on the
+host around the synchronous rebuild call. All of dompap's force methods map to
+the same GPU neighbour-list kernel, so ``test_double_loop`` only affects the
+report.
+"""
+from __future__ import annotations
+
+from time import perf_counter
+
+
+def autotune(sim, steps=100, test_double_loop=True, smallest_skin=0.1, step_skin=0.1, verbose=False,
+             plot=False):
+    sim_copy = sim.copy()
+    sim_copy.step()
+    results = {}
+    for method in ("double loop", "cell list"):
+        sim_copy.set_neighbor_list(method_str=method)
+        times = []
+        for _ in range(4):
+            tic = perf_counter()
+            sim_copy.update_neighbor_list(check=False)
+            times.append(perf_counter() - tic)
+        results[method] = min(times)
+        if verbose:
+            print(f"Time to update neighbor list ({method}): {results[method] * 1000:.3f} milliseconds")
+    fastest_method = min(results, key=results.get)
+    if verbose:
+        print(f"Fastest method to update neighbor list: {fastest_method}")
+    sim.neighbor_list_method_str = fastest_method
+    sim_copy.neighbor_list_method_str = fastest_method
+
+    largest_allowed_skin = min(sim.box_vectors) / 2
+    skins, times, updates = [], [], []
+    skin = smallest_skin
+    old_time = float("inf")
+    while skin < largest_allowed_skin:
+        before = sim_copy.number_of_neighbor_list_updates
+        sim_copy.set_neighbor_list(skin=skin)
+        ms = sim_copy.run_timed(steps)
+        skins.append(skin)
+        times.append(ms / 1000.0)
+        updates.append(sim_copy.number_of_neighbor_list_updates - before)
+        skin += step_skin
+        if ms / 1000.0 > old_time:
+            break
+        old_time = ms / 1000.0
+    if verbose:
+        print("Skin | Time per step (ms) | steps/updates")
+        for s, t, u in zip(skins, times, updates):
+            print(f"{s:4.2f} | {t / steps * 1000:8.5f}          | {steps}/{u}")
+    best = skins[times.index(min(times))] if skins else sim.neighbor_list_skin
+    if verbose:
+        print(f"Optimal parameters: skin={best}")
+    sim.set_neighbor_list(skin=best, method_str=fastest_method)
+    if plot:
+        try:
+            import matplotlib.pyplot as plt
+
+            plt.plot(skins, times, "o", label="Neighbour list")
+            plt.xlabel("Skin")
+            plt.ylabel("Time")
+            plt.legend()
+            plt.show()
+        except ImportError:
+            pass
+    return sim

@@ -1,0 +1,173 @@
+/*
+ * dompap_gpu.h — C ABI of the GB300 (sm_103a) molecular-dynamics hot path.
+ *
+ * One handle (dp_sim) holds one periodic system of N point particles in D
+ * dimensions (D = 2, 3 or 4) resident in GPU memory, plus its pair potential,
+ * neighbour list and integrator settings. Every entry point takes plain
+ * pointers and sizes; host arrays use dompap's own layouts (row-major (N, D)
+ * float64 positions etc.). Every entry point returns 0 (DP_OK) or a DP_ERR_*
+ * code; dp_last_error() then describes the failure. A handle is not
+ * thread-safe; distinct handles may be used from distinct threads.
+ *
+ * Each declaration names the dompap function it replaces (paths inside the
+ * dompap project, version 0.0.6). The Python `Simulation` in dompap_gb300 is
+ * the drop-in binding; INTEGRATION.md shows the ctypes stub dompap itself
+ * would add.
+ */
+#ifndef DOMPAP_GPU_H
+#define DOMPAP_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DP_OK 0
+#define DP_ERR_ARG 1        /* invalid argument / shape / state                  */
+#define DP_ERR_CUDA 2       /* CUDA runtime error                                */
+#define DP_ERR_NVRTC 3      /* the generated pair potential failed to compile    */
+#define DP_ERR_OVERFLOW 4   /* neighbour list exceeded max_number_of_neighbors   */
+#define DP_ERR_GEOMETRY 5   /* box too small for the single-image convention     */
+#define DP_ERR_NONFINITE 6  /* a force or position became NaN / Inf              */
+#define DP_ERR_NOPOT 7      /* no pair potential set                             */
+
+#define DP_PREC_FP64 0 /* float64 pair arithmetic (parity mode)                        */
+#define DP_PREC_FP32 1 /* float32 pair forces, float64 integration, wrap and sums      */
+
+#define DP_NL_CELL 0   /* cell list + Verlet list (falls back to all pairs if < 3 cells) */
+#define DP_NL_ALLPAIRS 1 /* O(N^2) build, rows in ascending index order                */
+
+#define DP_INT_GJF 0 /* Langevin G-JF leap-frog                         */
+#define DP_INT_NVE 1 /* NVE leap-frog                                   */
+
+#define DP_PAIR_CONST 0 /* sigma, epsilon constants                              */
+#define DP_PAIR_TYPES 1 /* (ntypes, ntypes) tables indexed by particle type      */
+#define DP_PAIR_DENSE 2 /* (N, N) matrices sigma[n, m] (index callables)         */
+
+typedef struct dp_sim dp_sim;
+
+typedef struct dp_stats {
+    int64_t steps;              /* integrated steps (RNG counter)                     */
+    int64_t rebuilds;           /* neighbour-list builds on the device                */
+    int32_t max_neighbors;      /* largest neighbour count of the current list        */
+    int32_t neighbor_capacity;  /* current per-particle list capacity                 */
+    int32_t cells[4];           /* cells per axis of the cell list (0: all pairs)     */
+    int32_t cell_capacity;      /* particles per cell slot array                      */
+    int32_t method_used;        /* DP_NL_CELL or DP_NL_ALLPAIRS                       */
+    double nl_cutoff;           /* largest sigma * r_cut + skin                       */
+} dp_stats;
+
+/* Last error message of the calling thread ("" if none). */
+const char *dp_last_error(void);
+/* ABI version (major * 10000 + minor * 100 + patch). */
+int dp_version(void);
+
+/* Create / destroy a system of n particles in dim dimensions on the current
+ * CUDA device. Replaces the state arrays of dompap/Simulation.py:101-147. */
+int dp_create(int dim, int64_t n, int precision, dp_sim **out);
+int dp_destroy(dp_sim *sim);
+int dp_set_precision(dp_sim *sim, int precision);
+
+/* State upload / download, (N, D) row-major float64 / int32 and (N,) arrays.
+ * Replaces direct assignment of Simulation.positions / velocities / betas /
+ * image_positions / masses / particle_types (dompap/Simulation.py:101-114,
+ * set_masses :232, set_types :292). */
+int dp_set_positions(dp_sim *sim, const double *positions);
+int dp_get_positions(dp_sim *sim, double *positions);
+int dp_set_velocities(dp_sim *sim, const double *velocities);
+int dp_get_velocities(dp_sim *sim, double *velocities);
+int dp_set_betas(dp_sim *sim, const double *betas);
+int dp_get_betas(dp_sim *sim, double *betas);
+int dp_set_images(dp_sim *sim, const int32_t *images);
+int dp_get_images(dp_sim *sim, int32_t *images);
+int dp_set_masses(dp_sim *sim, const double *masses);
+int dp_set_types(dp_sim *sim, const int32_t *types);
+/* Box side lengths (D,). Replaces Simulation.box_vectors / scale_box
+ * (dompap/Simulation.py:527-543). Forces a neighbour-list rebuild. */
+int dp_set_box(dp_sim *sim, const double *box);
+
+/* Pair potential: CUDA C++ source defining
+ *   template <typename R> __device__ R dp_pair_u(R s);  (u(s) - u(r_cut))
+ *   template <typename R> __device__ R dp_pair_f(R s);  (-du/ds)
+ *   template <typename R> __device__ R dp_pair_c(R s);  (d2u/ds2)
+ * generated from the SymPy expression by dompap_gb300.codegen; compiled with
+ * NVRTC for sm_103a. Replaces make_pair_potential (dompap/potential.py:43-66)
+ * and the hard-coded potentials (:10-40). Values are 0 where s > r_cut. */
+int dp_set_potential(dp_sim *sim, const char *device_source, double r_cut);
+/* sigma / epsilon: mode DP_PAIR_CONST (tables of 1), DP_PAIR_TYPES
+ * (ntypes x ntypes) or DP_PAIR_DENSE (N x N). Replaces
+ * set_pair_potential_parameters (dompap/Simulation.py:469-525). */
+int dp_set_pair_params(dp_sim *sim, int mode, int ntypes, const double *sigma, const double *epsilon);
+/* Skin, per-particle capacity and build method; forces a rebuild.
+ * Replaces set_neighbor_list (dompap/Simulation.py:307-381). */
+int dp_set_neighbor_list(dp_sim *sim, double skin, int max_neighbors, int method);
+/* Rebuild if any particle moved more than skin/2 since the last build
+ * (check != 0) or unconditionally (check == 0). *rebuilt (may be NULL) tells
+ * which. Replaces update_neighbor_list (dompap/Simulation.py:383-401) and
+ * neighbor_list_is_old (dompap/neighbor_list.py:183-201). */
+int dp_update_neighbor_list(dp_sim *sim, int check, int *rebuilt);
+/* Neighbour list in dompap's layout: (N, kmax) int32, rows ascending, -1
+ * padded. *max_count receives the largest row length (rows longer than kmax
+ * are truncated). Replaces Simulation.neighbor_list as built by
+ * get_neighbor_list_double_loop (dompap/neighbor_list.py:7-39). */
+int dp_get_neighbor_list(dp_sim *sim, int32_t *out, int kmax, int32_t *max_count);
+/* Positions at the last neighbour-list build, (N, D) row-major.
+ * Replaces Simulation.positions_neighbour_list (dompap/Simulation.py:381). */
+int dp_get_reference_positions(dp_sim *sim, double *positions);
+
+/* Integrator parameters. Replaces set_integrator (dompap/Simulation.py:739-759);
+ * seed keys the counter-based normal deviates. */
+int dp_set_integrator(dp_sim *sim, double time_step, double temperature, double damping_time, uint64_t seed);
+/* `steps` steps of integrator `kind` (DP_INT_GJF or DP_INT_NVE). Each step:
+ * neighbour-list check/rebuild, forces, integrate, wrap into box.
+ * Replaces Simulation.run / step / step_leap_frog (dompap/Simulation.py:681-737)
+ * with make_one_step / make_one_step_leap_frog (dompap/integrator.py:5-40)
+ * and wrap_into_box (dompap/positions.py:90-98). */
+int dp_run(dp_sim *sim, int64_t steps, int kind);
+/* Same as dp_run, also returning the device time of the steps in ms
+ * (CUDA events on the handle's stream). */
+int dp_run_timed(dp_sim *sim, int64_t steps, int kind, float *ms);
+
+/* Forces (N, D) row-major. Replaces get_forces (dompap/Simulation.py:594-619)
+ * -> _get_forces (dompap/potential.py:163-188). */
+int dp_forces(dp_sim *sim, double *forces);
+/* Potential energy. Replaces get_potential_energy -> _get_total_energy
+ * (dompap/Simulation.py:545-570, dompap/potential.py:69-100). */
+int dp_potential_energy(dp_sim *sim, double *energy);
+/* Pair virial W. Replaces get_virial -> _get_virial_double_loop
+ * (dompap/Simulation.py:946-967, dompap/potential.py:253-279). */
+int dp_virial(dp_sim *sim, double *virial);
+/* Per-particle Laplacian (N,). Replaces get_laplacian -> _get_laplacian
+ * (dompap/Simulation.py:1205-1229, dompap/potential.py:327-364). */
+int dp_laplacian(dp_sim *sim, double *laplacian);
+/* sum_n m_n |v_n|^2. Used by get_temperature / get_kinetic_energy /
+ * get_pressure (dompap/Simulation.py:817-836, 896-910, 969-988). */
+int dp_sum_mv2(dp_sim *sim, double *sum_mv2);
+/* u_cut, f_cut, c_cut of the compiled potential at n scaled distances
+ * (the callables returned by make_pair_potential, dompap/potential.py:61-66). */
+int dp_eval_potential(dp_sim *sim, const double *s, int64_t n, double *u, double *f, double *c);
+/* Standard normal deviates the G-JF step `step` draws, (N, D) row-major
+ * (the np.random.normal of dompap/integrator.py:30; test hook). */
+int dp_get_normals(dp_sim *sim, int64_t step, double *normals);
+
+/* Wrap positions into [0, L) and update the images in place. Replaces
+ * Simulation.wrap_into_box (dompap/Simulation.py:656-679, positions.py:90-98). */
+int dp_wrap(dp_sim *sim);
+/* Histogram of all ordered pair distances (i of type_a, j of type_b; -1 = all;
+ * self pairs included) with np.round minimum image over nbins bins with the
+ * nbins + 1 ascending edges (np.histogram semantics). The host normalises as
+ * get_radial_distribution_function (dompap/positions.py:58-87) does. */
+int dp_rdf_counts(dp_sim *sim, int type_a, int type_b, const double *edges, int nbins, uint64_t *counts);
+
+int dp_get_stats(dp_sim *sim, dp_stats *stats);
+/* Device time of `reps` launches of the force kernel on the current state
+ * (ms per launch, CUDA events on the handle's stream). */
+int dp_time_forces(dp_sim *sim, int reps, float *ms_per_launch);
+/* Number of kernels the last dp_run launched (graph nodes included). */
+int64_t dp_kernel_launches(dp_sim *sim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DOMPAP_GPU_H */

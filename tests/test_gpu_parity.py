@@ -1,0 +1,166 @@
+"""GPU parity with the reference: pair sets bit-exact, forces / energy / virial /
+Laplacian within 1e-10 relative (FP64 mode), on the golden configurations
+(produced by the unmodified reference) and on fresh seeded inputs checked by
+the oracle.
+
+Tolerances, FP64 mode: force relative RMS <= 1e-10; energy, virial within
+1e-10 of the sum of absolute pair terms; Laplacian max error <= 1e-10 of its
+largest magnitude. FP32-force mode: force relative RMS <= 1e-4 (stated per
+configuration in the test output).
+"""
+import numpy as np
+import pytest
+
+from conftest import CONFIG_TAGS, config_of
+from gpu_helpers import oracle_params, oracle_potential, rel_rms, sim_from_config
+from oracle import numpy_ref as ref
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+
+@pytest.mark.parametrize("method", ["double loop", "cell list"])
+@pytest.mark.parametrize("tag", CONFIG_TAGS)
+def test_golden_configuration(golden_configs, tag, method):
+    cfg = config_of(golden_configs, tag)
+    sim = sim_from_config(cfg, tag, method=method)
+    pos, box = cfg["positions"], cfg["box"]
+    # pair set, order and -1 padding as dompap's double loop
+    nl = sim.neighbor_list
+    k = cfg["nlist"].shape[1]
+    assert np.all(nl[:, k:] == -1)
+    assert np.array_equal(nl[:, :k], cfg["nlist"]), "pair set differs from the reference"
+    forces = sim.get_forces()
+    assert rel_rms(forces, cfg["forces"]) <= TOL
+    u, f, c = oracle_potential(cfg, tag)
+    sig, eps = oracle_params(cfg)
+    onl = cfg["nlist"]
+    if "energy" in cfg:
+        scale = ref.pair_terms_abs_sum(pos, box, u, onl, sig, eps)
+        assert abs(sim.get_potential_energy() - cfg["energy"]) <= TOL * max(scale, 1e-300)
+    _, w_abs = ref.virial_double_loop(pos, box, f, sig, eps, return_abs=True)
+    assert abs(sim.get_virial() - cfg["virial"]) <= TOL * max(w_abs, 1e-300)
+    lap = sim.get_laplacian()
+    assert np.max(np.abs(lap - cfg["laplacian"])) <= TOL * np.max(np.abs(cfg["laplacian"]))
+    assert abs(sim.get_temperature() - cfg["temperature"]) <= 1e-12 * cfg["temperature"]
+    assert abs(sim.get_kinetic_energy() - cfg["kinetic_energy"]) <= 1e-12 * cfg["kinetic_energy"]
+    assert abs(sim.get_pressure() - cfg["pressure"]) <= TOL * (abs(cfg["pressure"]) + w_abs / sim.get_volume())
+    if "rdf_g" in cfg:
+        r, g = sim.get_radial_distribution_function(cfg["rdf_bins"])
+        assert np.array_equal(r, cfg["rdf_r"])
+        np.testing.assert_allclose(g, cfg["rdf_g"], rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("tag", ["lj500", "harm3d", "harm2d", "harm4d", "wahn", "expensive"])
+def test_fp32_force_mode(golden_configs, tag):
+    cfg = config_of(golden_configs, tag)
+    sim = sim_from_config(cfg, tag, method="cell list", precision="fp32")
+    forces = sim.get_forces()
+    err = rel_rms(forces, cfg["forces"])
+    print(f"{tag}: FP32-force relative RMS error {err:.2e}")
+    assert err <= 1e-4
+    assert np.array_equal(sim.neighbor_list[:, : cfg["nlist"].shape[1]], cfg["nlist"])
+
+
+@pytest.mark.parametrize("dim,cells,density,seed", [(3, (6, 6, 6), 1.2, 1), (2, (30, 30), 1.1, 2),
+                                                    (4, (6, 6, 6, 6), 1.3, 3)])
+def test_fresh_inputs_against_oracle(dim, cells, density, seed):
+    """Seeded random configurations (not from the fixtures): GPU vs oracle."""
+    from dompap_gb300 import Simulation
+
+    rng = np.random.default_rng(seed)
+    sim = Simulation()
+    sim.set_positions(unit_cell_coordinates=([0.0] * dim,), cells=cells, lattice_constants=(1.0,) * dim)
+    sim.set_masses(masses=1.0)
+    sim.set_density(density=density)
+    sim.positions = sim.positions + rng.normal(0, 0.05, size=sim.positions.shape)
+    sim.wrap_into_box()
+    sim.set_pair_potential("(1-r)**2", 1.0)
+    sim.set_neighbor_list(skin=0.3, max_number_of_neighbors=64, method_str="cell list")
+    pos, box = np.array(sim.positions), np.array(sim.box_vectors)
+    nl_ref, _ = ref.neighbor_list_double_loop(pos, box, 1.3, 64)
+    assert np.array_equal(sim.neighbor_list, nl_ref)
+    u, f, c = ref.make_pair_potential("(1-r)**2", 1.0)
+    assert rel_rms(sim.get_forces(), ref.forces_neighbor_list(pos, box, f, nl_ref)) <= TOL
+    e = ref.energy_neighbor_list(pos, box, u, nl_ref)
+    assert abs(sim.get_potential_energy() - e) <= TOL * ref.pair_terms_abs_sum(pos, box, u, nl_ref)
+
+
+def test_edge_cases_pair_set():
+    """Reference unit-test geometry (tests/test_neighbor_list.py:12-51), an empty
+    neighbourhood, coincident boundary values and positions outside the box."""
+    from dompap_gb300 import Simulation
+
+    sim = Simulation()
+    sim.box_vectors = np.array([6.0, 6.0, 6.0])
+    sim.positions = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [2, 2, 2], [5, 5, 0]], dtype=np.float64)
+    sim.velocities = np.zeros((6, 3))
+    sim.betas = np.zeros((6, 3))
+    sim.image_positions = np.zeros((6, 3), dtype=np.int32)
+    sim.masses = np.ones((6, 1))
+    sim.particle_types = np.zeros((6, 1), dtype=np.int32)
+    sim.set_pair_potential("(1-r)**2", 0.5)
+    for method in ("double loop", "cell list"):
+        sim.set_neighbor_list(skin=1.0, max_number_of_neighbors=4, method_str=method)
+        assert np.array_equal(sim.neighbor_list, np.array([[1, 2, 3, 5], [0, 2, 3, -1], [0, 1, 3, -1],
+                                                           [0, 1, 2, -1], [-1, -1, -1, -1], [0, -1, -1, -1]]))
+    # positions left outside the box: the pair set follows the single-shift rule on raw coordinates
+    raw = np.array([[0, 0, 0], [7, 0, 0], [0, -5.5, 0], [0, 0, 1], [2, 2, 2], [5, 5, 0]], dtype=np.float64)
+    want, _ = ref.neighbor_list_double_loop(raw, np.array([6.0] * 3), 1.5, 8)
+    for method in ("double loop", "cell list"):
+        sim.positions = raw
+        sim.set_neighbor_list(skin=1.0, max_number_of_neighbors=8, method_str=method)
+        assert np.array_equal(sim.neighbor_list, want)
+
+
+def test_overflow_grows_capacity():
+    """max_number_of_neighbors set too small: dompap would write out of bounds;
+    here the list capacity grows and the pair set stays complete."""
+    from dompap_gb300 import Simulation
+
+    rng = np.random.default_rng(11)
+    sim = Simulation()
+    sim.set_positions(unit_cell_coordinates=([0.0, 0.0, 0.0],), cells=(8, 8, 8), lattice_constants=(1, 1, 1))
+    sim.set_masses(masses=1.0)
+    sim.set_density(density=1.0)
+    sim.positions = sim.positions + rng.normal(0, 0.05, size=sim.positions.shape)
+    sim.wrap_into_box()
+    sim.set_pair_potential("(1-r)**2", 1.0)
+    sim.set_neighbor_list(skin=0.6, max_number_of_neighbors=4, method_str="cell list")
+    pos, box = np.array(sim.positions), np.array(sim.box_vectors)
+    nl_ref, counts = ref.neighbor_list_double_loop(pos, box, 1.6, None)
+    assert counts.max() > 4
+    u, f, c = ref.make_pair_potential("(1-r)**2", 1.0)
+    assert rel_rms(sim.get_forces(), ref.forces_neighbor_list(pos, box, f, nl_ref)) <= TOL
+    sim.max_number_of_neighbors = np.int32(nl_ref.shape[1])
+    assert np.array_equal(sim.neighbor_list, nl_ref)
+
+
+def test_codegen_potential_values(golden_unit):
+    """The NVRTC-compiled potential at sample points vs the reference's callables."""
+    from dompap_gb300 import Simulation
+
+    sim = Simulation()
+    for tag, expr, rc in (("harm", "(1-r)**2", 1.0), ("lj", "4*(r**-12-r**-6)", 2.5),
+                          ("exp", str(golden_unit["pot_exp/expr"]), 3.0)):
+        sim.set_pair_potential(expr, rc)
+        r = golden_unit[f"pot_{tag}/r"]
+        for name, fn in (("u", sim.pair_potential), ("f", sim.pair_force), ("c", sim.pair_curvature)):
+            want = golden_unit[f"pot_{tag}/{name}"]
+            np.testing.assert_allclose(fn(r), want, rtol=1e-13, atol=1e-13 * np.max(np.abs(want)))
+    sim.set_pair_potential("Harmonic repulsive")
+    np.testing.assert_array_equal(sim.pair_potential(golden_unit["pot_hard/r"]), golden_unit["pot_hard/u"])
+    assert sim.pair_potential(0.5) == 0.125
+
+
+def test_bad_potential_raises():
+    from dompap_gb300 import Simulation
+    from dompap_gb300._lib import DompapGPUError
+
+    sim = Simulation()
+    with pytest.raises((ValueError, DompapGPUError, Exception)):
+        sim.set_pair_potential("(1-r)**2 + x", 1.0)
+    with pytest.raises(ValueError):
+        sim.set_neighbor_list(method_str="bogus")
+    with pytest.raises(ValueError):
+        sim.set_pair_potential("(1-r)**2", 1.0, force_method="bogus")
