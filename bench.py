@@ -1,0 +1,403 @@
+"""Benchmark of the molecular-dynamics step on GB300 (particle-steps/s).
+
+Default workload (N=1 GPU): 3-D harmonic repulsive u = (1-r)^2, r_cut = 1,
+fcc 64x64x64 cells = 1,048,576 particles at number density 1.0, positions
+jittered by N(0, 0.01) from a seed, Langevin G-JF with T = 0.002, dt = 0.01,
+damping time 0.1, neighbour-list skin 0.2, float64 pair arithmetic ("plain"
+FP64 path). One step = skin test (+ neighbour-list rebuild when due) + pair
+forces + G-JF integrate + wrap for all particles.
+
+``value`` is device time (CUDA events on the library's stream) of exactly
+``--steps`` steps after ``--warmup`` untimed steps; ``e2e`` drives the same
+step through the C ABI with host buffers: every step uploads positions,
+velocities and betas from pinned host memory and reads the positions back.
+``--impl reference`` times the reference's algorithm for the same workload on
+the host cores (the C/OpenMP restatement in ``oracle/cport``: prange loops
+parallel, the rest serial as in dompap).
+
+Multi-GPU: the path does not shard a single system (replicas only); under
+torchrun every rank runs its own replica and ``value`` is the sum.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+FCC = ((0.0, 0.0, 0.0), (0.5, 0.5, 0.0), (0.5, 0.0, 0.5), (0.0, 0.5, 0.5))
+METRIC = "particle-steps/s on 1 GB300: plain vs batched/MLP-surrogate at stated force error"
+UNIT = "particle-steps/s"
+
+WORKLOADS = {
+    # name: (dim, unit cell, cells, density, potential, r_cut, skin, T, dt, tau, jitter)
+    "harmonic3d": (3, FCC, (64, 64, 64), 1.0, "(1-r)**2", 1.0, 0.2, 0.002, 0.01, 0.1, 0.01),
+    "harmonic2d": (2, ((0.0, 0.0),), (1024, 1024), 1.0, "(1-r)**2", 1.0, 0.2, 0.002, 0.01, 0.1, 0.01),
+    "harmonic4d": (4, ((0.0, 0.0, 0.0, 0.0),), (32, 32, 32, 32), 1.0, "(1-r)**2", 1.0, 0.2, 0.002, 0.01, 0.1, 0.01),
+    "lj500": (3, FCC, (5, 5, 5), 0.8442, "4*(r**-12-r**-6)", 2.5, 0.5, 1.0, 0.005, 0.1, 0.0),
+}
+
+
+def host_state(name, seed):
+    """Lattice + jitter + Maxwell-Boltzmann velocities, as dompap builds it
+    (set_positions -> set_density -> jitter -> wrap)."""
+    from dompap_gb300.positions import generate_positions
+
+    dim, unit, cells, rho, pot, rc, skin, T, dt, tau, jitter = WORKLOADS[name]
+    pos = generate_positions(unit, cells, (1.0,) * dim)
+    box = np.array(cells, dtype=np.float64)
+    scale = (pos.shape[0] / np.prod(box) / rho) ** (1 / dim)
+    box = box * scale
+    pos = pos * scale
+    rng = np.random.default_rng(seed)
+    if jitter:
+        pos = pos + rng.normal(0.0, jitter, size=pos.shape)
+    shift = np.floor(pos / box)
+    img = shift.astype(np.int32)
+    pos = pos - shift * box
+    vel = rng.normal(0.0, np.sqrt(T), size=pos.shape)
+    return pos, vel, img, box
+
+
+def build_sim(name, seed, precision="fp64"):
+    from dompap_gb300 import Simulation
+
+    dim, unit, cells, rho, pot, rc, skin, T, dt, tau, jitter = WORKLOADS[name]
+    pos, vel, img, box = host_state(name, seed)
+    np.random.seed(seed)
+    sim = Simulation(precision=precision)
+    n = pos.shape[0]
+    sim.box_vectors = box
+    sim.positions = pos
+    sim.velocities = vel
+    sim.betas = np.zeros_like(pos)
+    sim.image_positions = img
+    sim.masses = np.ones((n, 1))
+    sim.particle_types = np.zeros((n, 1), dtype=np.int32)
+    sim.set_pair_potential(pot, rc)
+    sim.set_neighbor_list(skin=skin, max_number_of_neighbors=64 if dim < 4 else 96, method_str="cell list")
+    sim.set_integrator(time_step=dt, target_temperature=T, temperature_damping_time=tau)
+    return sim
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def kernel_times(sim, reps=50):
+    from dompap_gb300 import _lib
+
+    lib = _lib.load()
+    out = {}
+    for name, which in (("forces", _lib.DP_KERNEL_FORCES), ("gjf_integrate", _lib.DP_KERNEL_GJF),
+                        ("rebuild", _lib.DP_KERNEL_REBUILD), ("skin_check", _lib.DP_KERNEL_SKIN)):
+        ms = _lib.ctypes.c_float(0.0)
+        r = reps if which != _lib.DP_KERNEL_REBUILD else max(3, reps // 10)
+        _lib.check(lib.dp_time_kernel(sim._h, which, r, _lib.ctypes.byref(ms)))
+        out[name] = float(ms.value)
+    return out
+
+
+def e2e_run(sim, steps):
+    """C-ABI step with host buffers: upload pos/vel/beta from pinned memory,
+    one step, download positions; device time from host clock with syncs."""
+    import torch
+
+    from dompap_gb300 import _lib
+
+    lib = _lib.load()
+    h = sim._h
+    n, d = np.asarray(sim.positions).shape
+
+    def pinned():
+        return torch.empty((n, d), dtype=torch.float64, pin_memory=True).numpy()
+
+    pos, vel, beta = pinned(), pinned(), pinned()
+    out = pinned()
+    _lib.check(lib.dp_get_positions(h, _lib.dptr(pos)))
+    _lib.check(lib.dp_get_velocities(h, _lib.dptr(vel)))
+    _lib.check(lib.dp_get_betas(h, _lib.dptr(beta)))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        _lib.check(lib.dp_set_positions(h, _lib.dptr(pos)))
+        _lib.check(lib.dp_set_velocities(h, _lib.dptr(vel)))
+        _lib.check(lib.dp_set_betas(h, _lib.dptr(beta)))
+        _lib.check(lib.dp_run(h, 1, _lib.DP_INT_GJF))
+        _lib.check(lib.dp_get_positions(h, _lib.dptr(out)))
+    dt = time.perf_counter() - t0
+    sim._mark_device_newer()
+    return n * steps / dt, 3 * n * d * 8, n * d * 8
+
+
+# ------------------------------------------------------------------ CPU port
+def cpu_port_run(name, steps, warmup, seed, max_seconds=None):
+    """Reference algorithm on the host cores: per step skin test (serial),
+    neighbour-list rebuild when due (dompap's serial 3-D cell list, or the
+    prange double loop for D != 3), prange force loop, serial G-JF and wrap."""
+    from oracle.cport import build as cport
+
+    dim, unit, cells, rho, pot, rc, skin, T, dt, tau, jitter = WORKLOADS[name]
+    lib = cport.load()
+    fptr = cport.compile_potential(pot, rc)
+    pos, vel, img, box = host_state(name, seed)
+    n = pos.shape[0]
+    kmax = 16 if dim == 3 else (8 if dim == 2 else 24)
+    if name == "lj500":
+        kmax = 128
+    nl = np.full((n, kmax), -1, dtype=np.int32)
+    beta = np.zeros_like(pos)
+    force = np.zeros_like(pos)
+    mass = np.ones(n)
+    scratch = np.zeros(n * dim)
+    ref_pos = pos.copy()
+    cutoff = rc + skin
+    lib.dp_port_seed(seed)
+
+    def P(a):
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+    def I(a):  # noqa: E743
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+    def rebuild():
+        if dim == 3 and name != "lj500":
+            lib.dp_port_nl_cell_list_3d(P(pos), n, P(box), cutoff, kmax, I(nl))
+        else:
+            lib.dp_port_nl_double_loop(P(pos), n, dim, P(box), cutoff, kmax, I(nl))
+        ref_pos[:] = pos
+
+    def step():
+        rebuilt = 0
+        if lib.dp_port_nl_is_old(P(pos), P(ref_pos), n, dim, P(box), skin):
+            rebuild()
+            rebuilt = 1
+        lib.dp_port_forces(P(pos), n, dim, P(box), I(nl), kmax, fptr, 1.0, 1.0, P(force))
+        lib.dp_port_gjf(P(pos), P(vel), P(beta), P(force), P(mass), n, dim, dt, T, tau, P(scratch))
+        lib.dp_port_wrap(P(pos), I(img), n, dim, P(box))
+        return rebuilt
+
+    t_build0 = time.perf_counter()
+    rebuild()
+    t_build = time.perf_counter() - t_build0
+    for _ in range(warmup):
+        step()
+    rebuilds = 0
+    done = 0
+    t0 = time.perf_counter()
+    while done < steps:
+        rebuilds += step()
+        done += 1
+        if max_seconds is not None and time.perf_counter() - t0 > max_seconds:
+            break
+    t = time.perf_counter() - t0
+    return {"steps": done, "seconds": t, "rebuilds": rebuilds, "build_seconds": t_build, "n": n,
+            "threads": lib.dp_port_threads()}
+
+
+def cpu_baseline(name, seed, gpu_steps_per_rebuild):
+    """Bounded sample (about 10-30 s) of the CPU port; the rebuild cost is
+    amortised with the steps-per-rebuild the GPU run measured."""
+    r = cpu_port_run(name, steps=1000000, warmup=1, seed=seed, max_seconds=12.0)
+    per_step = (r["seconds"] - r["rebuilds"] * r["build_seconds"]) / r["steps"]
+    per_step = max(per_step, 1e-12) + r["build_seconds"] / max(gpu_steps_per_rebuild, 1.0)
+    return {"value": r["n"] / per_step, "unit": UNIT, "cores": r["threads"], "kind": "port",
+            "sample": (f"{r['steps']} full steps of the same {r['n']}-particle system on the host "
+                       f"(C/OpenMP restatement of dompap's loops, prange loops on {r['threads']} threads), "
+                       f"rebuild {r['build_seconds']:.2f} s amortised over {gpu_steps_per_rebuild:.1f} "
+                       "steps/rebuild measured on the GPU")}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    name = args.workload
+    r = cpu_port_run(name, steps=args.steps, warmup=args.warmup, seed=args.seed, max_seconds=90.0)
+    value = r["n"] * r["steps"] / r["seconds"]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": r["steps"], "warmup": args.warmup, "ms_per_step": 1000 * r["seconds"] / r["steps"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded lattice + N(0,0.01) jitter)",
+        "config": config_of(name),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["threads"], "kind": "port",
+                         "sample": (f"{r['steps']} full MD steps (rebuilds {r['rebuilds']} included) of the "
+                                    f"{r['n']}-particle system; C/OpenMP restatement of dompap's loops "
+                                    "(Numba is not installed); capped at 90 s of timed work")},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def config_of(name):
+    dim, unit, cells, rho, pot, rc, skin, T, dt, tau, jitter = WORKLOADS[name]
+    n = int(np.prod(cells)) * len(unit)
+    return {"workload": name, "dim": dim, "particles": n, "lattice": f"{len(unit)}-point basis x {cells}",
+            "density": rho, "pair_potential": pot, "r_cut": rc, "skin": skin, "temperature": T, "time_step": dt,
+            "damping_time": tau, "jitter_sigma": jitter, "precision": "fp64 pair arithmetic",
+            "l2": "working set > L2 (state + list ~ 0.2 GB for 1M particles, no flush)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="harmonic3d", choices=sorted(WORKLOADS))
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    sim = build_sim(args.workload, args.seed + rank)
+    n = sim.number_of_particles()
+    sim.run(args.warmup)
+    st0 = sim._stats()
+    barrier()
+    with ClockSampler(local) as clocks:
+        ms = sim.run_timed(args.steps)
+    barrier()
+    st1 = sim._stats()
+    from dompap_gb300 import _lib
+
+    launches = int(_lib.load().dp_kernel_launches(sim._h))
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = n * args.steps * world / (ms_max / 1000.0)
+    rebuilds = int(st1.rebuilds - st0.rebuilds)
+    steps_per_rebuild = args.steps / max(rebuilds, 1)
+
+    # per-kernel device times (same state) for the roofline
+    kt = kernel_times(sim)
+    mean_k = float(np.mean(np.sum(np.asarray(sim.neighbor_list) != -1, axis=1))) if n <= 4_000_000 else 12.0
+    dim = sim.get_dimensions_of_space()
+    alg = {
+        "forces": 4 * mean_k + 16 * dim + 4,  # SURVEY per-particle bytes: list + count + own x + F write
+        "gjf_integrate": 72 * dim + 8,        # read x, v, beta, F, x_ref, mass, image; write x, v, beta, image
+    }
+    dominant = max(alg, key=lambda k: kt[k])
+    peak, peak_kind = measured_peaks()
+    achieved = alg[dominant] * n / (kt[dominant] / 1000.0) / 1e9
+    e2e_value, h2d, d2h = e2e_run(sim, args.e2e_steps)
+    e2e_total = torch.tensor([e2e_value], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(e2e_total, op=dist.ReduceOp.SUM)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded lattice + N(0,0.01) jitter, MB velocities)",
+        "config": dict(config_of(args.workload), parallelism=f"replicas x{world}" if world > 1 else "single system"),
+        "clocks": clocks.summary(),
+        "gpu_launches": launches,
+        "e2e": {"value": float(e2e_total.item()), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_particle": alg[dominant]},
+        "kernel_ms": kt, "mean_neighbors": mean_k, "rebuilds_in_timed_region": rebuilds,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.workload, args.seed, steps_per_rebuild)
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

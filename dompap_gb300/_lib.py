@@ -33,6 +33,11 @@ DP_INT_NVE = 1
 DP_PAIR_CONST = 0
 DP_PAIR_TYPES = 1
 DP_PAIR_DENSE = 2
+DP_KERNEL_FORCES = 0
+DP_KERNEL_GJF = 1
+DP_KERNEL_NVE = 2
+DP_KERNEL_REBUILD = 3
+DP_KERNEL_SKIN = 4
 
 _ERROR_NAMES = {
     DP_ERR_ARG: "invalid argument",
@@ -108,6 +113,7 @@ _SIGNATURES = {
     "dp_rdf_counts": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _D, ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_uint64)]),
     "dp_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(DpStats)]),
+    "dp_time_kernel": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "dp_time_forces": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "dp_kernel_launches": (ctypes.c_int64, [_P]),
 }

@@ -1692,7 +1692,7 @@ int dp_potential_energy(dp_sim* s, double* energy) {
 int dp_virial(dp_sim* s, double* virial) {
     double w = 0.0;
     RET(scalar_pair(s, s ? s->lib.virial : nullptr, &w));
-    *virial = w / 2 / s->dim;
+    *virial = w / s->dim;
     return DP_OK;
 }
 
@@ -1787,20 +1787,40 @@ int dp_get_stats(dp_sim* s, dp_stats* st) {
     return DP_OK;
 }
 
-int dp_time_forces(dp_sim* s, int reps, float* ms) {
+int dp_time_kernel(dp_sim* s, int which, int reps, float* ms) {
     RET(require_ready(s));
     if (!ms || reps < 1) return fail(DP_ERR_ARG, "bad arguments");
     RET(update_nl(s, true, nullptr));
-    RET(launch_pair(s, s->lib.forces, s->force, nullptr));  // warm-up
+    RET(ensure_partial(s, grid_for(s->n, kBlock)));
+    auto once = [&]() -> int {
+        switch (which) {
+            case DP_KERNEL_FORCES: return launch_pair(s, s->lib.forces, s->force, nullptr);
+            case DP_KERNEL_GJF: return launch_integrate(s, DP_INT_GJF, 0, nullptr);
+            case DP_KERNEL_NVE: return launch_integrate(s, DP_INT_NVE, 0, nullptr);
+            case DP_KERNEL_REBUILD:
+                k_set_rebuild<<<1, 1, 0, s->stream>>>(s->dstat);
+                return launch_rebuild(s, nullptr);
+            case DP_KERNEL_SKIN: return launch_skin_check(s);
+            default: return fail(DP_ERR_ARG, "unknown kernel");
+        }
+    };
+    RET(once());  // warm-up
     CK(cudaEventRecord(s->ev0, s->stream));
-    for (int r = 0; r < reps; ++r) RET(launch_pair(s, s->lib.forces, s->force, nullptr));
+    for (int r = 0; r < reps; ++r) RET(once());
     CK(cudaEventRecord(s->ev1, s->stream));
     CK(cudaEventSynchronize(s->ev1));
     float t = 0.0f;
     CK(cudaEventElapsedTime(&t, s->ev0, s->ev1));
     *ms = t / reps;
+    // leave a consistent list behind (the integrator kernels moved particles)
+    RET(read_status(s));
+    s->hstat->need_rebuild = 1;
+    RET(write_status(s));
+    RET(update_nl(s, true, nullptr));
     return DP_OK;
 }
+
+int dp_time_forces(dp_sim* s, int reps, float* ms) { return dp_time_kernel(s, DP_KERNEL_FORCES, reps, ms); }
 
 int dp_wrap(dp_sim* s) {
     if (!s) return fail(DP_ERR_ARG, "null handle");

@@ -12,7 +12,7 @@
 // Semantics follow dompap's neighbour-list kernels:
 //   force      dompap/potential.py:163-188  F_n = sum_m eps f(r/sigma) d/r
 //   energy     dompap/potential.py:69-100   U = 1/2 sum_n sum_m eps u(r/sigma)
-//   virial     dompap/potential.py:253-279  W = 1/D sum_{n<m} eps f(r/sigma) r
+//   virial     dompap/potential.py:253-279  W = 1/D sum_{n<m} eps(n,m) f(r/sigma(n,m)) r (pairs m > n of each list)
 //   laplacian  dompap/potential.py:327-364  sum_m eps c(r/sigma) - (D-1) eps f(r/sigma)/r
 // with s = r / sigma and every term 0 where s > r_cut (dompap/potential.py:61-65).
 // There is no 1/sigma chain-rule factor, exactly as in the reference.
@@ -81,6 +81,9 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
     const int32_t* __restrict__ row = a.nl + i;
     for (int kk = 0; kk < c; ++kk) {
         const int j = __ldg(row + (long long)kk * n);
+        // the virial is the reference's upper-triangle sum over n < m with
+        // sigma(n, m), epsilon(n, m) (dompap/potential.py:265-278)
+        if (ACC == DP_ACC_VIRIAL && j <= i) continue;
         uint32_t uj[D];
         dp_shadow_unpack<D>(__ldg(sh + j), uj);
         float df[D];

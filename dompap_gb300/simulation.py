@@ -151,12 +151,11 @@ class Simulation:
     def __setattr__(self, name, value):
         if name in _STATE or name in _HOST_ONLY:
             d = self.__dict__
-            if name == "image_positions":
-                value = np.ascontiguousarray(value, dtype=np.int32)
-            elif name == "particle_types":
-                value = np.ascontiguousarray(value, dtype=np.int32)
+            # always a private copy: device results are written into it in place
+            if name in ("image_positions", "particle_types"):
+                value = np.array(value, dtype=np.int32, order="C")
             else:
-                value = np.array(value, dtype=np.float64)
+                value = np.array(value, dtype=np.float64, order="C")
             d["_" + name] = value
             d["_dev_newer"].discard(name)
             d["_host_dirty"].add(name)

@@ -161,8 +161,16 @@ int dp_wrap(dp_sim *sim);
 int dp_rdf_counts(dp_sim *sim, int type_a, int type_b, const double *edges, int nbins, uint64_t *counts);
 
 int dp_get_stats(dp_sim *sim, dp_stats *stats);
-/* Device time of `reps` launches of the force kernel on the current state
- * (ms per launch, CUDA events on the handle's stream). */
+#define DP_KERNEL_FORCES 0  /* pair forces                                */
+#define DP_KERNEL_GJF 1     /* G-JF integrate + wrap + skin test            */
+#define DP_KERNEL_NVE 2     /* NVE integrate + wrap + skin test             */
+#define DP_KERNEL_REBUILD 3 /* forced neighbour-list rebuild (all kernels)  */
+#define DP_KERNEL_SKIN 4    /* skin test alone                              */
+/* Device time of `reps` back-to-back launches of one step kernel on the
+ * current state (ms per launch, CUDA events on the handle's stream). The
+ * integrator variants advance the state; the list is rebuilt afterwards. */
+int dp_time_kernel(dp_sim *sim, int which, int reps, float *ms_per_launch);
+/* dp_time_kernel(sim, DP_KERNEL_FORCES, reps, ms_per_launch). */
 int dp_time_forces(dp_sim *sim, int reps, float *ms_per_launch);
 /* Number of kernels the last dp_run launched (graph nodes included). */
 int64_t dp_kernel_launches(dp_sim *sim);

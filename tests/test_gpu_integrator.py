@@ -170,9 +170,9 @@ def test_copy_is_independent():
 
     sim = Simulation()
     cp = sim.copy()
-    cp.positions[0] = [1.0, 0.0, 0.0]
+    cp.positions[0] = [0.5, 0.0, 0.0]
     assert np.array_equal(sim.positions[:3], [[0, 0, 0], [0, 0, 1], [0, 0, 2]])
-    assert np.array_equal(cp.positions[:3], [[1, 0, 0], [0, 0, 1], [0, 0, 2]])
+    assert np.array_equal(cp.positions[:3], [[0.5, 0, 0], [0, 0, 1], [0, 0, 2]])
     cp.run(5)
     assert np.array_equal(sim.positions[:1], [[0, 0, 0]])
 
