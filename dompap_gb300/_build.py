@@ -82,9 +82,9 @@ def build_library(verbose: bool = False) -> str:
 
 
 SAMPLE_POTENTIAL = """
-template <typename R> __device__ __forceinline__ R dp_pair_u(R s) { R t = R(1) - s; return t * t; }
-template <typename R> __device__ __forceinline__ R dp_pair_f(R s) { return R(2) * (R(1) - s); }
-template <typename R> __device__ __forceinline__ R dp_pair_c(R s) { return R(2); }
+template <typename R> __device__ __forceinline__ R dp_pair_u(R s, R) { R t = R(1) - s; return t * t; }
+template <typename R> __device__ __forceinline__ R dp_pair_f(R s, R) { return R(2) * (R(1) - s); }
+template <typename R> __device__ __forceinline__ R dp_pair_c(R s, R) { return R(2); }
 """
 
 

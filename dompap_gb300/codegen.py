@@ -4,14 +4,16 @@ Replaces ``make_pair_potential`` (dompap/potential.py:43-66): the expression
 string in ``r`` is parsed with SymPy, ``f = -du/dr`` and ``c = d2u/dr2`` are
 derived symbolically, and the three are printed as templated device functions
 
-    template <typename R> __device__ R dp_pair_u(R r);   // u(r) - u(r_cut)
-    template <typename R> __device__ R dp_pair_f(R r);   // -du/dr
-    template <typename R> __device__ R dp_pair_c(R r);   // d2u/dr2
+    template <typename R> __device__ R dp_pair_u(R r, R dp_inv_r);   // u(r) - u(r_cut)
+    template <typename R> __device__ R dp_pair_f(R r, R dp_inv_r);   // -du/dr
+    template <typename R> __device__ R dp_pair_c(R r, R dp_inv_r);   // d2u/dr2
 
 that ``pair_kernels.cuh`` inlines into its neighbour loops (the cut ``r >
-r_cut -> 0`` is applied there). ``R`` is ``double`` in FP64 mode and ``float``
-in FP32 mode, so every literal is printed as ``R(...)``. Integer powers become
-multiplication chains (negative powers share one reciprocal), half-integer
+r_cut -> 0`` is applied there). ``dp_inv_r`` is ``1/r``, which the kernels get
+from one reciprocal square root together with ``r``; negative integer powers
+of ``r`` are printed as powers of it, so they cost no division. ``R`` is
+``double`` in FP64 mode and ``float`` in FP32 mode, so every literal is printed
+as ``R(...)``. Integer powers become multiplication chains, half-integer
 powers go through ``sqrt``, everything else calls the CUDA math library.
 
 The value shift ``u(r_cut)`` is evaluated the way the reference evaluates it —
@@ -35,9 +37,9 @@ HARDCODED = {
 }
 
 _HARDCODED_SOURCE = """
-template <typename R> __device__ __forceinline__ R dp_pair_u(R r) { return r < R(1) ? R(0.5) * (R(1) - r) * (R(1) - r) : R(0); }
-template <typename R> __device__ __forceinline__ R dp_pair_f(R r) { return r < R(1) ? R(1) - r : R(0); }
-template <typename R> __device__ __forceinline__ R dp_pair_c(R r) { return R(0); }
+template <typename R> __device__ __forceinline__ R dp_pair_u(R r, R) { return r < R(1) ? R(0.5) * (R(1) - r) * (R(1) - r) : R(0); }
+template <typename R> __device__ __forceinline__ R dp_pair_f(R r, R) { return r < R(1) ? R(1) - r : R(0); }
+template <typename R> __device__ __forceinline__ R dp_pair_c(R r, R) { return R(0); }
 """
 
 _PRELUDE = """
@@ -112,7 +114,7 @@ class _CudaPrinter(C99CodePrinter):
 
 
 def _share_reciprocal(expr: sp.Expr) -> tuple[sp.Expr, bool]:
-    """Rewrite r**(-n) as dp_inv_r**n so all negative powers share one division."""
+    """Rewrite r**(-n) as dp_inv_r**n (1/r is an argument of the device function)."""
     used = False
 
     def repl(e):
@@ -128,11 +130,9 @@ def _share_reciprocal(expr: sp.Expr) -> tuple[sp.Expr, bool]:
 
 def _function_source(name: str, expr: sp.Expr, shift_literal: str | None = None) -> str:
     printer = _CudaPrinter()
-    expr, uses_inv = _share_reciprocal(expr)
+    expr, _ = _share_reciprocal(expr)
     repl, reduced = sp.cse(expr, symbols=sp.numbered_symbols("dp_t"))
-    lines = [f"template <typename R> __device__ __forceinline__ R {name}(R r) {{"]
-    if uses_inv:
-        lines.append("    const R dp_inv_r = R(1) / r;")
+    lines = [f"template <typename R> __device__ __forceinline__ R {name}(R r, R dp_inv_r) {{"]
     for sym, sub in repl:
         lines.append(f"    const R {sym} = {printer.doprint(sub)};")
     body = printer.doprint(reduced[0])

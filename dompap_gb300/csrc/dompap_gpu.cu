@@ -102,41 +102,77 @@ __global__ void k_soa_to_aos_i32(const int32_t* __restrict__ in, int32_t* __rest
 struct ShadowArgs {
     const double* pos;
     void* shadow;
+    dp_dev_status* st;
     long long n;
     double scale[DP_MAX_DIM];
+    double box[DP_MAX_DIM];
 };
 
+// Fixed-point shadow of all positions; flags coordinates outside
+// [-L/4, 5L/4), for which the single-shift image is not the nearest one.
 template <int D>
 __global__ void k_shadow(ShadowArgs a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     uint32_t u[D];
+    bool far = false;
 #pragma unroll
-    for (int k = 0; k < D; ++k) u[k] = dp_fixed(a.pos[k * a.n + i], a.scale[k]);
+    for (int k = 0; k < D; ++k) {
+        const double x = a.pos[k * a.n + i];
+        u[k] = dp_fixed(x, a.scale[k]);
+        far = far || !(x >= -0.25 * a.box[k] && x < 1.25 * a.box[k]);
+    }
     ((typename dp_shadow_t<D>::type*)a.shadow)[i] = dp_shadow_pack<D>(u);
+    if (far) atomicExch(&a.st->far, 1);
 }
 
 // --------------------------- skin test ------------------------------------
 // neighbor_list_is_old (dompap/neighbor_list.py:183-201): rebuild when some
 // particle's min-image displacement^2 since the last build exceeds (skin/2)^2.
+// The displacement since the last build is read from the fixed-point shadows
+// in float32; only when it lies within the error bound of (skin/2)^2 is it
+// recomputed in float64 exactly as the reference does.
 struct SkinArgs {
     const double* pos;
     const double* pos_ref;
+    const void* shadow;
+    const void* shadow_ref;
     dp_dev_status* st;
     long long n;
     double box[DP_MAX_DIM];
-    double thr;  // (0.5 * skin)^2
+    float unit[DP_MAX_DIM];
+    double thr;    // (0.5 * skin)^2
+    float thr_lo;  // below: certainly not old
+    float thr_hi;  // above: certainly old
 };
+
+template <int D>
+__device__ __forceinline__ bool skin_old(const SkinArgs& a, long long i, const uint32_t* u, const double* x) {
+    typedef typename dp_shadow_t<D>::type sh_t;
+    uint32_t uref[D];
+    dp_shadow_unpack<D>(((const sh_t*)a.shadow_ref)[i], uref);
+    float df[D];
+    const float qf = dp_shadow_q<D>(u, uref, a.unit, df);
+    if (qf <= a.thr_lo) return false;
+    if (qf > a.thr_hi) return true;
+    double d[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) d[k] = dp_min_image(x[k] - a.pos_ref[k * a.n + i], a.box[k]);
+    return dp_sqsum_exact<D>(d) > a.thr;
+}
 
 template <int D>
 __global__ void k_skin_check(SkinArgs a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     bool old = false;
     if (i < a.n) {
-        double d[D];
+        typedef typename dp_shadow_t<D>::type sh_t;
+        uint32_t u[D];
+        dp_shadow_unpack<D>(((const sh_t*)a.shadow)[i], u);
+        double x[D];
 #pragma unroll
-        for (int k = 0; k < D; ++k) d[k] = dp_min_image(a.pos[k * a.n + i] - a.pos_ref[k * a.n + i], a.box[k]);
-        old = dp_sqsum_exact<D>(d) > a.thr;
+        for (int k = 0; k < D; ++k) x[k] = a.pos[k * a.n + i];
+        old = skin_old<D>(a, i, u, x);
     }
     if (__any_sync(0xffffffffu, old) && (threadIdx.x & 31) == 0) atomicExch(&a.st->need_rebuild, 1);
 }
@@ -234,6 +270,8 @@ __global__ void k_cell_sort(CellArgs a) {
 struct NlArgs {
     const double* pos;
     double* pos_ref;
+    const void* shadow;
+    void* shadow_ref;
     int32_t* nl;
     int32_t* cnt;
     const int32_t* cell_cnt;
@@ -245,7 +283,10 @@ struct NlArgs {
     int nc[DP_MAX_DIM];
     double inv_w[DP_MAX_DIM];
     double box[DP_MAX_DIM];
+    float unit[DP_MAX_DIM];
     double cutoff;
+    float lo2;  // float32 r^2 below this: certainly inside the cutoff
+    float hi2;  // float32 r^2 above this: certainly outside
 };
 
 template <int D>
@@ -253,10 +294,16 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_cells(NlArgs a) {
     if (!a.st->need_rebuild) return;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
+    typedef typename dp_shadow_t<D>::type sh_t;
+    const sh_t* sh = (const sh_t*)a.shadow;
+    const bool far = a.st->far != 0;
     const long long n = a.n;
     double xi[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) xi[k] = a.pos[k * n + i];
+    const sh_t shi = sh[i];
+    uint32_t ui[D];
+    dp_shadow_unpack<D>(shi, ui);
     int ci[D];
     cell_coords<D>(xi, a.nc, a.inv_w, a.box, ci);
     int count = 0;
@@ -280,10 +327,21 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_cells(NlArgs a) {
         for (int t = 0; t < m; ++t) {
             const int j = mem[t];
             if (j == i) continue;
-            double d[D];
+            // float32 pre-test on the fixed-point displacement (nearest image,
+            // never longer than the single-shift one); float64 only near the cutoff
+            uint32_t uj[D];
+            dp_shadow_unpack<D>(__ldg(sh + j), uj);
+            float df[D];
+            const float qf = dp_shadow_q<D>(ui, uj, a.unit, df);
+            if (qf > a.hi2) continue;
+            bool inside = qf < a.lo2 && !far;
+            if (!inside) {
+                double d[D];
 #pragma unroll
-            for (int k = 0; k < D; ++k) d[k] = dp_min_image(xi[k] - a.pos[k * n + j], a.box[k]);
-            if (sqrt(dp_sqsum_exact<D>(d)) < a.cutoff) {
+                for (int k = 0; k < D; ++k) d[k] = dp_min_image(xi[k] - a.pos[k * n + j], a.box[k]);
+                inside = sqrt(dp_sqsum_exact<D>(d)) < a.cutoff;
+            }
+            if (inside) {
                 if (count < a.kcap) a.nl[(long long)count * n + i] = j;
                 ++count;
             }
@@ -293,6 +351,7 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_cells(NlArgs a) {
     atomicMax(&a.st->max_neighbors, count);
 #pragma unroll
     for (int k = 0; k < D; ++k) a.pos_ref[k * n + i] = xi[k];
+    ((sh_t*)a.shadow_ref)[i] = shi;
 }
 
 // All-pairs build for boxes with fewer than 3 cells per axis; rows come out in
@@ -334,6 +393,8 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_allpairs(NlArgs a) {
     atomicMax(&a.st->max_neighbors, count);
 #pragma unroll
     for (int k = 0; k < D; ++k) a.pos_ref[k * n + i] = xi[k];
+    typedef typename dp_shadow_t<D>::type sh_t;
+    ((sh_t*)a.shadow_ref)[i] = ((const sh_t*)a.shadow)[i];
 }
 
 __global__ void k_rebuild_done(dp_dev_status* st) {
@@ -388,6 +449,7 @@ struct IntArgs {
     int32_t* img;
     void* shadow;
     const double* pos_ref;
+    const void* shadow_ref;
     const uint8_t* mclass;
     const double* mcoef;  // [class][5]: a, b*dt/m, b/(2m), sqrt(2 alpha T dt), dt/m
     const double* mass;   // MASSMODE 2
@@ -395,7 +457,9 @@ struct IntArgs {
     long long n;
     double box[DP_MAX_DIM];
     double scale[DP_MAX_DIM];
+    float unit[DP_MAX_DIM];
     double thr;  // (skin/2)^2
+    float thr_lo, thr_hi;
     double dt;
     double coef[5];  // MASSMODE 0
     double temperature;
@@ -446,11 +510,15 @@ __device__ __forceinline__ double wrap_axis(double x, double L, int32_t& image) 
 }
 
 // Langevin G-JF leap-frog (dompap/integrator.py:17-40, arXiv:1303.7011
-// Sec. II.C eqs. 16-17), then wrap, fixed-point shadow and the skin test for
-// the next step.
+// Sec. II.C eqs. 16-17) or NVE leap-frog (:5-14), then the wrap into the box,
+// the fixed-point shadow and the skin test for the next step. The float64
+// position is converted to fixed point once; a value outside [0, 2^32) is the
+// only case that needs the wrap (done exactly as wrap_into_box), and the skin
+// test reads the shadows (float64 only near the threshold).
 template <int D, int MASSMODE, bool NVE>
 __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->far = 0;  // every position is wrapped below
     bool old = false, bad = false;
     if (i < a.n) {
         const long long n = a.n;
@@ -459,7 +527,7 @@ __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
         float z[4];
         if (!NVE) dp_normals4(a.seed, (unsigned long long)(a.st->step + a.step_offset), (uint32_t)i, z);
         uint32_t u[D];
-        double q = 0.0;
+        double xs[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
             const long long o = k * n + i;
@@ -474,19 +542,34 @@ __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
                 a.beta[o] = bn;
             }
             x = x + v * a.dt;
-            int32_t im = a.img[o];
-            const int32_t im0 = im;
-            x = wrap_axis(x, a.box[k], im);
-            if (im != im0) a.img[o] = im;
+            const long long t = __double2ll_rd(x * a.scale[k]);
+            if (t < 0 || t >= 4294967296LL) {
+                int32_t im = a.img[o];
+                x = wrap_axis(x, a.box[k], im);
+                a.img[o] = im;
+                u[k] = dp_fixed(x, a.scale[k]);
+                bad = bad || !isfinite(x);
+            } else {
+                u[k] = (uint32_t)t;
+            }
             a.vel[o] = v;
             a.pos[o] = x;
-            u[k] = dp_fixed(x, a.scale[k]);
-            const double d = dp_min_image(x - a.pos_ref[o], a.box[k]);
-            q = (k == 0) ? __dmul_rn(d, d) : __dadd_rn(q, __dmul_rn(d, d));
-            bad = bad || !isfinite(x);
+            xs[k] = x;
         }
         ((typename dp_shadow_t<D>::type*)a.shadow)[i] = dp_shadow_pack<D>(u);
-        old = q > a.thr;
+        SkinArgs sa;
+        sa.pos_ref = a.pos_ref;
+        sa.shadow_ref = a.shadow_ref;
+        sa.n = n;
+        sa.thr = a.thr;
+        sa.thr_lo = a.thr_lo;
+        sa.thr_hi = a.thr_hi;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            sa.box[k] = a.box[k];
+            sa.unit[k] = a.unit[k];
+        }
+        old = skin_old<D>(sa, i, u, xs);
     }
     const bool any_old = __any_sync(0xffffffffu, old);
     const bool any_bad = __any_sync(0xffffffffu, bad);
@@ -542,6 +625,7 @@ __global__ void k_normals(unsigned long long seed, long long step, double* out, 
 template <int D>
 __global__ void k_wrap(IntArgs a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->far = 0;
     if (i >= a.n) return;
     uint32_t u[D];
 #pragma unroll
@@ -706,6 +790,7 @@ struct dp_sim {
     double *pos = nullptr, *vel = nullptr, *beta = nullptr, *force = nullptr, *pos_ref = nullptr;
     int32_t* img = nullptr;
     void* shadow = nullptr;
+    void* shadow_ref = nullptr;
     size_t shadow_bytes = 0;
     double *bk_pos = nullptr, *bk_vel = nullptr, *bk_beta = nullptr;
     int32_t* bk_img = nullptr;
@@ -735,7 +820,7 @@ struct dp_sim {
     int pmode = DP_PAIR_CONST;
     int ntypes = 1;
     double sigma = 1.0, epsilon = 1.0, sig_max = 1.0;
-    double *sig_tab = nullptr, *eps_tab = nullptr;
+    double *sig_tab = nullptr, *eps_tab = nullptr, *isig_tab = nullptr;
 
     // neighbour list
     double skin = 1.0;
@@ -810,12 +895,33 @@ static void fill_scale(const dp_sim* s, double* scale, float* unit) {
     }
 }
 
+// Largest fixed-point unit L / 2^32 over the axes times sqrt(D): the absolute
+// error bound (with a factor 4 margin) of a float32 distance from the shadows.
+static double shadow_abs_error(const dp_sim* s) {
+    double lmax = 0.0;
+    for (int k = 0; k < s->dim; ++k) lmax = std::max(lmax, s->box[k]);
+    return 4.0 * lmax / 4294967296.0 * std::sqrt((double)s->dim);
+}
+
+// float32 squared-distance thresholds bracketing a float64 distance `r`:
+// below lo the distance is certainly < r, above hi certainly > r.
+static void bracket(const dp_sim* s, double r, float* lo2, float* hi2) {
+    const double e = shadow_abs_error(s);
+    const double lo = (r - e) * (1.0 - 1e-5);
+    const double hi = (r + e) * (1.0 + 1e-5);
+    *lo2 = lo > 0.0 ? (float)(lo * lo) * (1.0f - 1e-6f) : -1.0f;
+    *hi2 = std::isfinite(hi) ? (float)(hi * hi) * (1.0f + 1e-6f) : INFINITY;
+}
+
 static int launch_shadow(dp_sim* s) {
     ShadowArgs a{};
     a.pos = s->pos;
     a.shadow = s->shadow;
+    a.st = s->dstat;
     a.n = s->n;
     fill_scale(s, a.scale, nullptr);
+    for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
+    CK(cudaMemsetAsync(&s->dstat->far, 0, sizeof(int32_t), s->stream));
     const unsigned g = grid_for(s->n, kBlock);
     switch (s->dim) {
         case 2: k_shadow<2><<<g, kBlock, 0, s->stream>>>(a); break;
@@ -924,6 +1030,8 @@ static int launch_rebuild(dp_sim* s, long long* launches) {
     NlArgs na{};
     na.pos = s->pos;
     na.pos_ref = s->pos_ref;
+    na.shadow = s->shadow;
+    na.shadow_ref = s->shadow_ref;
     na.nl = s->nl;
     na.cnt = s->cnt;
     na.cell_cnt = s->cell_cnt;
@@ -933,6 +1041,8 @@ static int launch_rebuild(dp_sim* s, long long* launches) {
     na.kcap = s->kcap;
     na.ccap = s->ccap;
     na.cutoff = s->cutoff;
+    bracket(s, s->cutoff, &na.lo2, &na.hi2);
+    fill_scale(s, nullptr, na.unit);
     for (int k = 0; k < DP_MAX_DIM; ++k) na.box[k] = (k < s->dim) ? s->box[k] : 1.0;
     long long nl_launches = 0;
     if (s->use_cells) {
@@ -979,6 +1089,7 @@ static void fill_pair_args(const dp_sim* s, dp_pair_args& a, double* out) {
     a.types = s->types;
     a.sig_tab = s->sig_tab;
     a.eps_tab = s->eps_tab;
+    a.isig_tab = s->isig_tab;
     a.out = out;
     a.partial = s->partial;
     a.status = s->dstat;
@@ -987,6 +1098,7 @@ static void fill_pair_args(const dp_sim* s, dp_pair_args& a, double* out) {
     for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
     fill_scale(s, nullptr, a.unit);
     a.sigma = s->sigma;
+    a.inv_sigma = 1.0 / s->sigma;
     a.epsilon = s->epsilon;
     a.rcut = s->r_cut;
     // Pre-filter threshold: a pair is skipped only when its float32 distance,
@@ -1021,14 +1133,16 @@ static void fill_int_args(const dp_sim* s, IntArgs& a, long long step_offset) {
     a.img = s->img;
     a.shadow = s->shadow;
     a.pos_ref = s->pos_ref;
+    a.shadow_ref = s->shadow_ref;
     a.mclass = s->mclass;
     a.mcoef = s->mcoef;
     a.mass = s->mass;
     a.st = s->dstat;
     a.n = s->n;
     for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
-    fill_scale(s, a.scale, nullptr);
+    fill_scale(s, a.scale, a.unit);
     a.thr = (0.5 * s->skin) * (0.5 * s->skin);
+    bracket(s, 0.5 * s->skin, &a.thr_lo, &a.thr_hi);
     a.dt = s->dt;
     {
         const double m = s->class_mass[0];
@@ -1078,10 +1192,14 @@ static int launch_skin_check(dp_sim* s) {
     SkinArgs a{};
     a.pos = s->pos;
     a.pos_ref = s->pos_ref;
+    a.shadow = s->shadow;
+    a.shadow_ref = s->shadow_ref;
     a.st = s->dstat;
     a.n = s->n;
     for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
+    fill_scale(s, nullptr, a.unit);
     a.thr = (0.5 * s->skin) * (0.5 * s->skin);
+    bracket(s, 0.5 * s->skin, &a.thr_lo, &a.thr_hi);
     const unsigned g = grid_for(s->n, kBlock);
     switch (s->dim) {
         case 2: k_skin_check<2><<<g, kBlock, 0, s->stream>>>(a); break;
@@ -1328,7 +1446,12 @@ int dp_create(int dim, int64_t n, int precision, dp_sim** out) {
         (rc = dalloc_t(&s->bk_img, nd)) || (rc = dalloc_t(&s->cnt, (size_t)n)))
         return cleanup();
     s->shadow_bytes = (size_t)n * (dim == 2 ? 8 : 16);
-    if ((rc = dalloc(&s->shadow, s->shadow_bytes))) return cleanup();
+    if ((rc = dalloc(&s->shadow, s->shadow_bytes)) || (rc = dalloc(&s->shadow_ref, s->shadow_bytes))) return cleanup();
+    if (cudaMemset(s->shadow, 0, s->shadow_bytes) != cudaSuccess ||
+        cudaMemset(s->shadow_ref, 0, s->shadow_bytes) != cudaSuccess) {
+        rc = fail(DP_ERR_CUDA, "cudaMemset failed");
+        return cleanup();
+    }
     if (cudaMemset(s->pos, 0, nd * 8) != cudaSuccess || cudaMemset(s->vel, 0, nd * 8) != cudaSuccess ||
         cudaMemset(s->beta, 0, nd * 8) != cudaSuccess || cudaMemset(s->force, 0, nd * 8) != cudaSuccess ||
         cudaMemset(s->pos_ref, 0, nd * 8) != cudaSuccess || cudaMemset(s->img, 0, nd * 4) != cudaSuccess ||
@@ -1356,9 +1479,10 @@ int dp_destroy(dp_sim* s) {
     if (!s) return DP_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_graphs(s);
-    void* bufs[] = {s->pos, s->vel, s->beta, s->force, s->pos_ref, s->img, s->shadow, s->bk_pos, s->bk_vel,
-                    s->bk_beta, s->bk_img, s->mclass, s->mcoef, s->class_mass_dev, s->mass, s->types, s->sig_tab,
-                    s->eps_tab, s->nl, s->cnt, s->cell_cnt, s->cell_mem, s->dstat, s->partial, s->dsum};
+    void* bufs[] = {s->pos, s->vel, s->beta, s->force, s->pos_ref, s->img, s->shadow, s->shadow_ref, s->bk_pos,
+                    s->bk_vel, s->bk_beta, s->bk_img, s->mclass, s->mcoef, s->class_mass_dev, s->mass, s->types,
+                    s->sig_tab, s->eps_tab, s->isig_tab, s->nl, s->cnt, s->cell_cnt, s->cell_mem, s->dstat,
+                    s->partial, s->dsum};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (s->hstat) cudaFreeHost(s->hstat);
@@ -1577,10 +1701,14 @@ int dp_set_pair_params(dp_sim* s, int mode, int ntypes, const double* sigma, con
         if (s->max_type >= ntypes) return fail(DP_ERR_ARG, "a particle type exceeds the per-type parameter table");
         const size_t m = (size_t)ntypes * ntypes;
         for (size_t t = 0; t < m; ++t) smax = std::max(smax, sigma[t]);
+        std::vector<double> inv(m);
+        for (size_t t = 0; t < m; ++t) inv[t] = 1.0 / sigma[t];
         RET(dalloc_t(&s->sig_tab, m));
         RET(dalloc_t(&s->eps_tab, m));
+        RET(dalloc_t(&s->isig_tab, m));
         CK(cudaMemcpy(s->sig_tab, sigma, m * sizeof(double), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(s->eps_tab, epsilon, m * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(s->isig_tab, inv.data(), m * sizeof(double), cudaMemcpyHostToDevice));
         s->ntypes = ntypes;
     } else if (mode == DP_PAIR_DENSE) {
         const size_t m = (size_t)s->n * s->n;
@@ -1804,6 +1932,8 @@ int dp_time_kernel(dp_sim* s, int which, int reps, float* ms) {
             default: return fail(DP_ERR_ARG, "unknown kernel");
         }
     };
+    const bool moves = which == DP_KERNEL_GJF || which == DP_KERNEL_NVE;
+    if (moves) RET(backup_state(s));
     RET(once());  // warm-up
     CK(cudaEventRecord(s->ev0, s->stream));
     for (int r = 0; r < reps; ++r) RET(once());
@@ -1812,7 +1942,9 @@ int dp_time_kernel(dp_sim* s, int which, int reps, float* ms) {
     float t = 0.0f;
     CK(cudaEventElapsedTime(&t, s->ev0, s->ev1));
     *ms = t / reps;
-    // leave a consistent list behind (the integrator kernels moved particles)
+    // the integrator kernels moved the particles: put the state back and
+    // leave a consistent list behind
+    if (moves) RET(restore_state(s));
     RET(read_status(s));
     s->hstat->need_rebuild = 1;
     RET(write_status(s));

@@ -22,6 +22,8 @@ struct dp_dev_status {
     int32_t max_neighbors;    // largest neighbour count seen by the last build
     int32_t cell_overflow;    // largest cell occupancy seen when it exceeded capacity
     int32_t nonfinite;        // a force or position became NaN/Inf
+    int32_t far;              // some coordinate lies outside [-L/4, 5L/4) (not yet wrapped)
+    int32_t pad;
     int64_t rebuilds;         // neighbour-list builds done on the device
     int64_t step;             // steps integrated (the RNG counter)
 };
@@ -36,6 +38,7 @@ struct dp_pair_args {
     const int32_t* types;
     const double* sig_tab;
     const double* eps_tab;
+    const double* isig_tab;  // 1 / sigma per type pair (DP_PMODE == 1)
     double* out;
     double* partial;
     dp_dev_status* status;
@@ -45,6 +48,7 @@ struct dp_pair_args {
     double box[DP_MAX_DIM];
     float unit[DP_MAX_DIM];  // L / 2^32 per axis
     double sigma;            // DP_PMODE == 0
+    double inv_sigma;        // DP_PMODE == 0
     double epsilon;          // DP_PMODE == 0
     double rcut;             // r_cut in units of sigma
     float cut2f;             // pre-filter: skip a pair when its float32 r^2 exceeds this

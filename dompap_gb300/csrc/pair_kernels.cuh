@@ -5,9 +5,9 @@
 // prepends the DP_* configuration macros, dp_common.cuh and the device
 // functions generated from the SymPy pair potential:
 //
-//   template <typename R> __device__ R dp_pair_u(R s);   // u(s) - u(r_cut)
-//   template <typename R> __device__ R dp_pair_f(R s);   // -du/ds
-//   template <typename R> __device__ R dp_pair_c(R s);   // d2u/ds2
+//   template <typename R> __device__ R dp_pair_u(R s, R inv_s);   // u(s) - u(r_cut)
+//   template <typename R> __device__ R dp_pair_f(R s, R inv_s);   // -du/ds
+//   template <typename R> __device__ R dp_pair_c(R s, R inv_s);   // d2u/ds2
 //
 // Semantics follow dompap's neighbour-list kernels:
 //   force      dompap/potential.py:163-188  F_n = sum_m eps f(r/sigma) d/r
@@ -38,16 +38,19 @@ typedef DP_REAL real_t;
 typedef typename dp_shadow_t<DP_DIM>::type shadow_t;
 
 __device__ __forceinline__ void dp_pair_params(const dp_pair_args& a, long long i, int ti, int j, double& sig,
-                                               double& eps) {
+                                               double& isig, double& eps) {
 #if DP_PMODE == 0
     sig = a.sigma;
+    isig = a.inv_sigma;
     eps = a.epsilon;
 #elif DP_PMODE == 1
     const int tj = __ldg(a.types + j);
     sig = __ldg(a.sig_tab + ti * a.ntypes + tj);
+    isig = __ldg(a.isig_tab + ti * a.ntypes + tj);
     eps = __ldg(a.eps_tab + ti * a.ntypes + tj);
 #else
     sig = __ldg(a.sig_tab + i * a.n + j);
+    isig = 1.0 / sig;
     eps = __ldg(a.eps_tab + i * a.n + j);
 #endif
 }
@@ -89,62 +92,79 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
         float df[D];
         const float qf = dp_shadow_q<D>(ui, uj, a.unit, df);
         if (qf > a.cut2f) continue;  // certainly beyond r_cut * sigma_max
-        double sig, eps;
-        dp_pair_params(a, i, ti, j, sig, eps);
+        double sig, isig, eps;
+        dp_pair_params(a, i, ti, j, sig, isig, eps);
 #if DP_REAL_IS_FLOAT
         // FP32 pair arithmetic on the fixed-point displacement.
-        const float r = sqrtf(qf);
+        const float rinv = rsqrtf(qf);
+        const float r = qf * rinv;
 #if DP_SIGMA_ONE
-        const float s = r;
+        const float s = r, sinv = rinv;
 #else
-        const float s = r / (float)sig;
+        const float s = r * (float)isig, sinv = rinv * (float)sig;
 #endif
         if (s > (float)a.rcut) continue;
         const float e = (float)eps;
         if (ACC == DP_ACC_FORCE) {
 #if DP_EPS_ONE
-            const float sf = dp_pair_f<float>(s);
+            const float sf = dp_pair_f<float>(s, sinv);
 #else
-            const float sf = e * dp_pair_f<float>(s);
+            const float sf = e * dp_pair_f<float>(s, sinv);
 #endif
-            const float g = sf / r;
+            const float g = sf * rinv;
 #pragma unroll
             for (int k = 0; k < D; ++k) acc_v[k] = fmaf(g, df[k], acc_v[k]);
         } else if (ACC == DP_ACC_ENERGY) {
-            acc_s += (double)(e * dp_pair_u<float>(s));
+            acc_s += (double)(e * dp_pair_u<float>(s, sinv));
         } else if (ACC == DP_ACC_VIRIAL) {
-            acc_s += (double)(e * dp_pair_f<float>(s) * r);
+            acc_s += (double)(e * dp_pair_f<float>(s, sinv) * r);
         } else {
-            acc_s += (double)(e * dp_pair_c<float>(s) + (float)(D - 1) * (-e * dp_pair_f<float>(s)) / r);
+            acc_s += (double)(e * dp_pair_c<float>(s, sinv) + (float)(D - 1) * (-e * dp_pair_f<float>(s, sinv)) * rinv);
         }
 #else
-        // FP64 pair arithmetic, reference order of operations.
+        // FP64 pair arithmetic. d and r^2 follow the reference exactly; 1/r
+        // comes from one reciprocal square root (no divisions), and where s
+        // lies within a few ulp of r_cut, r = sqrt(r^2) and s = r / sigma are
+        // recomputed with IEEE operations so the cut decision is the
+        // reference's.
         double d[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) d[k] = dp_min_image(xi[k] - __ldg(a.pos + k * n + j), a.box[k]);
         const double q = dp_sqsum_exact<D>(d);
-        const double r = sqrt(q);
+        const double rinv = rsqrt(q);
+        double r = q * rinv;
 #if DP_SIGMA_ONE
-        const double s = r;
+        double s = r;
+        const double sinv = rinv;
 #else
-        const double s = r / sig;
+        double s = r * isig;
+        const double sinv = rinv * sig;
 #endif
+        if (fabs(s - a.rcut) <= 1e-14 * a.rcut) {
+            r = sqrt(q);
+#if DP_SIGMA_ONE
+            s = r;
+#else
+            s = r / sig;
+#endif
+        }
         if (s > a.rcut) continue;
         if (ACC == DP_ACC_FORCE) {
 #if DP_EPS_ONE
-            const double sf = dp_pair_f<double>(s);
+            const double sf = dp_pair_f<double>(s, sinv);
 #else
-            const double sf = eps * dp_pair_f<double>(s);
+            const double sf = eps * dp_pair_f<double>(s, sinv);
 #endif
+            const double g = sf * rinv;
 #pragma unroll
-            for (int k = 0; k < D; ++k) acc_v[k] += sf * (d[k] / r);
+            for (int k = 0; k < D; ++k) acc_v[k] = fma(g, d[k], acc_v[k]);
         } else if (ACC == DP_ACC_ENERGY) {
-            acc_s += eps * dp_pair_u<double>(s);
+            acc_s += eps * dp_pair_u<double>(s, sinv);
         } else if (ACC == DP_ACC_VIRIAL) {
-            acc_s += eps * dp_pair_f<double>(s) * r;
+            acc_s += eps * dp_pair_f<double>(s, sinv) * r;
         } else {
-            const double sf = eps * dp_pair_f<double>(s);
-            acc_s += eps * dp_pair_c<double>(s) + (double)(D - 1) * (-sf) / r;
+            const double sf = eps * dp_pair_f<double>(s, sinv);
+            acc_s += eps * dp_pair_c<double>(s, sinv) + (double)(D - 1) * (-sf) * rinv;
         }
 #endif
     }
@@ -206,7 +226,8 @@ extern "C" __global__ void dp_eval_pair(const double* s_in, double* u, double* f
         c[i] = 0.0;
         return;
     }
-    u[i] = (double)dp_pair_u<real_t>((real_t)s);
-    f[i] = (double)dp_pair_f<real_t>((real_t)s);
-    c[i] = (double)dp_pair_c<real_t>((real_t)s);
+    const real_t sr = (real_t)s, sinv = real_t(1) / sr;
+    u[i] = (double)dp_pair_u<real_t>(sr, sinv);
+    f[i] = (double)dp_pair_f<real_t>(sr, sinv);
+    c[i] = (double)dp_pair_c<real_t>(sr, sinv);
 }
