@@ -721,6 +721,43 @@ __global__ void __launch_bounds__(kBlock) k_rdf(RdfArgs a) {
 }  // namespace
 
 // ===========================================================================
+// allocation-free kinetic sum (see dp_sum_mv2_noalloc in dompap_gpu.h)
+// ===========================================================================
+// Scratch for the per-block partial sums, one double per block of kBlock
+// particles: 16384 blocks = 128 KiB, i.e. at most 4,194,304 particles per
+// call. It lives in every GPU that loads this library until the process
+// exits. Every call shares it and overwrites exactly the partials it reads,
+// so nothing carries over between calls; calls that overlap on the GPU (two
+// streams at once) race on it.
+#define DP_NOALLOC_MAX_BLOCKS 16384
+static __device__ __align__(256) double g_noalloc_partial[DP_NOALLOC_MAX_BLOCKS];
+
+namespace {
+__global__ void __launch_bounds__(kBlock) k_mv2_rowmajor(const double* __restrict__ vel,
+                                                          const double* __restrict__ mass, long long n, int dim,
+                                                          double* __restrict__ partial) {
+    __shared__ double smem[32];
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < n) {
+        double s = 0.0;
+        for (int k = 0; k < dim; ++k) {
+            const double vk = vel[i * dim + k];
+            s += vk * vk;
+        }
+        v = mass[i] * s;
+    }
+    v = dp_block_sum(v, smem);
+    if (threadIdx.x == 0) partial[blockIdx.x] = v;
+}
+}  // namespace
+
+// Device address of g_noalloc_partial, looked up once per device (host code
+// cannot use the symbol itself: on the host it only names a stand-in).
+static std::mutex g_noalloc_mutex;
+static double* g_noalloc_addr[64] = {nullptr};
+
+// ===========================================================================
 // NVRTC pair-kernel libraries
 // ===========================================================================
 struct PairLib {
@@ -2023,6 +2060,37 @@ int dp_rdf_counts(dp_sim* s, int type_a, int type_b, const double* edges, int nb
     cudaFree(dedges);
     cudaFree(dcounts);
     if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("dp_rdf_counts: ") + cudaGetErrorString(e));
+    return DP_OK;
+}
+
+int dp_sum_mv2_noalloc(const double* velocities, const double* masses, int64_t n, int dim, double* out,
+                       void* stream) {
+    if (!velocities || !masses || !out) return fail(DP_ERR_ARG, "null device pointer");
+    if (dim < 1 || dim > DP_MAX_DIM) return fail(DP_ERR_ARG, "dimension must be in [1, 4]");
+    if (n < 1) return fail(DP_ERR_ARG, "number of particles must be >= 1");
+    const long long blocks = (n + kBlock - 1) / kBlock;
+    if (blocks > DP_NOALLOC_MAX_BLOCKS)
+        return fail(DP_ERR_ARG, "dp_sum_mv2_noalloc: " + std::to_string(n) + " particles exceed its fixed scratch (at most " +
+                                    std::to_string((long long)DP_NOALLOC_MAX_BLOCKS * kBlock) + ")");
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(DP_ERR_ARG, "device ordinal out of range");
+    double* partial = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_addr[dev]) {
+            void* p = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partial);
+            if (e != cudaSuccess || !p)
+                return fail(DP_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_partial): ") + cudaGetErrorString(e));
+            g_noalloc_addr[dev] = (double*)p;
+        }
+        partial = g_noalloc_addr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    k_mv2_rowmajor<<<(unsigned)blocks, kBlock, 0, st>>>(velocities, masses, n, dim, partial);
+    k_reduce<<<1, 1024, 0, st>>>(partial, blocks, out);
+    CK(cudaGetLastError());
     return DP_OK;
 }
 

@@ -172,6 +172,20 @@ int dp_get_stats(dp_sim *sim, dp_stats *stats);
 int dp_time_kernel(dp_sim *sim, int which, int reps, float *ms_per_launch);
 /* dp_time_kernel(sim, DP_KERNEL_FORCES, reps, ms_per_launch). */
 int dp_time_forces(dp_sim *sim, int reps, float *ms_per_launch);
+/* sum_n m_n |v_n|^2 like dp_sum_mv2, but on caller-owned device arrays and
+ * without allocating anything; it has no counterpart in the reference.
+ * For callers that cannot call cudaMalloc: code recording a CUDA graph (an
+ * allocation is not allowed during stream capture), and hosts that own all
+ * device memory through their own pool allocator. velocities: device (N, dim)
+ * row-major float64; masses: device (N,); out: device, one double; stream:
+ * a cudaStream_t (NULL = default stream). Asynchronous on `stream`.
+ * Scratch: a fixed 128 KiB device array inside this library, so N is at most
+ * 4,194,304 (larger N returns DP_ERR_ARG). The first call on a device looks
+ * up that array's address; make it before any stream capture. Calls share
+ * the array: calls that overlap on the GPU race. */
+int dp_sum_mv2_noalloc(const double *velocities, const double *masses, int64_t n, int dim, double *out,
+                       void *stream);
+
 /* Number of kernels the last dp_run launched (graph nodes included). */
 int64_t dp_kernel_launches(dp_sim *sim);
 
