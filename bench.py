@@ -300,6 +300,94 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
+def fp32_variant(name, seed, steps, warmup):
+    """The same workload with float32 pair forces (float64 integration, wrap and
+    sums): throughput and the force error against float64 on the same state."""
+    sim = build_sim(name, seed, precision="fp32")
+    n = sim.number_of_particles()
+    sim.run(warmup)
+    ms = sim.run_timed(steps)
+    kt = kernel_times(sim, reps=20)
+    f32 = sim.get_forces()
+    sim.set_precision("fp64")
+    f64 = sim.get_forces()
+    err = float(np.sqrt(np.mean((f32 - f64) ** 2) / max(np.mean(f64 ** 2), 1e-300)))
+    del sim
+    return {"value": n * steps / (ms / 1000.0), "unit": UNIT, "steps": steps, "ms_per_step": ms / steps,
+            "force_rel_rms_error_vs_fp64": err, "kernel_ms": kt}
+
+
+def batched_variant(seed, steps=40, warmup=5, loop_sample=16):
+    """4,096 LJ replicas (N log-uniform in [64, 8192] rounded to fcc 4abc, T
+    uniform in [0.7, 2.0], density 0.8442) in one persistent kernel, float32
+    forces / float64 integration, autotuned launch shape; against a Python loop
+    of per-replica single-system runs (float32 forces) on a random sample."""
+    from dompap_gb300 import Simulation
+    from dompap_gb300.batched import Replicas, lj_replica_specs
+    from oracle import numpy_ref as ref
+
+    specs, rejected = lj_replica_specs(4096, seed)
+    reps = Replicas(specs, "4*(r**-12-r**-6)", 2.5, time_step=0.005, damping_time=0.1, seed=seed)
+    best, _ = reps.autotune(steps=5, candidates=[(1024, 128, 512), (1024, 256, 512), (2048, 256, 512),
+                                                  (512, 128, 256), (1024, 128, 256)])
+    reps.run(warmup)
+    ms = reps.run(steps)
+    value = reps.ntot * steps / (ms / 1000.0)
+    # force error of the float32 kernel against the float64 oracle on sampled replicas
+    pos0, _, _ = reps.state()
+    reps.run(1, record_forces=True)
+    forces = reps.last_forces()
+    rng = np.random.default_rng(seed)
+    u, f, _ = ref.make_pair_potential("4*(r**-12-r**-6)", 2.5)
+    errs = []
+    for r in rng.choice(reps.n_rep, size=6, replace=False):
+        sl = reps.replica_slice(int(r))
+        nl, _ = ref.neighbor_list_double_loop(pos0[sl], reps.boxes[r], 2.5, None)
+        want = ref.forces_neighbor_list(pos0[sl], reps.boxes[r], f, nl)
+        errs.append(float(np.sqrt(np.mean((forces[sl] - want) ** 2) / np.mean(want ** 2))))
+    # per-replica launch loop (the dompap way: one system at a time) on a sample
+    loop_particles, loop_seconds = 0, 0.0
+    for r in rng.choice(reps.n_rep, size=loop_sample, replace=False):
+        sp = specs[int(r)]
+        n = sp.positions.shape[0]
+        sim = Simulation(precision="fp32")
+        sim.box_vectors = sp.box
+        sim.positions = sp.positions
+        sim.velocities = sp.velocities
+        sim.betas = np.zeros_like(sp.positions)
+        sim.image_positions = np.zeros(sp.positions.shape, dtype=np.int32)
+        sim.masses = np.ones((n, 1))
+        sim.particle_types = np.zeros((n, 1), dtype=np.int32)
+        sim.set_pair_potential("4*(r**-12-r**-6)", 2.5)
+        sim.set_neighbor_list(skin=min(0.5, float(np.min(sp.box)) / 2 - 2.5), method_str="cell list")
+        sim.set_integrator(time_step=0.005, target_temperature=sp.temperature, temperature_damping_time=0.1)
+        sim.run(warmup)
+        t0 = time.perf_counter()
+        sim.run(steps)
+        loop_seconds += time.perf_counter() - t0
+        loop_particles += n * steps
+        del sim
+    return {"value": value, "unit": UNIT, "steps": steps, "ms_per_step": ms / steps, "replicas": reps.n_rep,
+            "particles": reps.ntot, "rejected_draws_box_below_2rcut": rejected,
+            "launch_shape": {"split_n": best[0], "threads_small": best[1], "threads_large": best[2]},
+            "force_rel_rms_error_vs_fp64_oracle_max": max(errs),
+            "per_replica_loop": {"value": loop_particles / loop_seconds, "unit": UNIT,
+                                 "sample_replicas": loop_sample,
+                                 "how": "host loop of single-system runs (float32 forces, CUDA graphs per run)"}}
+
+
+def variants(args, main_sim):
+    out = {}
+    for name, fn in (("fp32_force", lambda: fp32_variant(args.workload, args.seed + 7, min(args.steps, 1000),
+                                                         args.warmup)),
+                     ("batched_4096_lj", lambda: batched_variant(args.seed + 11))):
+        try:
+            out[name] = fn()
+        except Exception as exc:  # reported, not hidden
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"}
+    return out
+
+
 def config_of(name):
     dim, unit, cells, rho, pot, rc, skin, T, dt, tau, jitter = WORKLOADS[name]
     n = int(np.prod(cells)) * len(unit)
@@ -319,6 +407,7 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--no-variants", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -393,6 +482,8 @@ def main():
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.workload, args.seed, steps_per_rebuild)
+    if rank == 0 and not args.no_variants:
+        line["variants"] = variants(args, sim)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:

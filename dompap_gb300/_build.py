@@ -40,7 +40,8 @@ def _cuda_home(nvcc: str) -> str:
 def write_embedded() -> str:
     os.makedirs(BUILD, exist_ok=True)
     parts = []
-    for name, sym in (("dp_common.cuh", "dp_src_common"), ("pair_kernels.cuh", "dp_src_pair")):
+    for name, sym in (("dp_common.cuh", "dp_src_common"), ("pair_kernels.cuh", "dp_src_pair"),
+                      ("batch_kernels.cuh", "dp_src_batch")):
         with open(os.path.join(CSRC, name)) as fh:
             text = fh.read()
         if ')DPSRC"' in text:
@@ -96,13 +97,15 @@ def check_pair_kernels(verbose: bool = True) -> None:
         common = fh.read()
     with open(os.path.join(CSRC, "pair_kernels.cuh")) as fh:
         pair = fh.read()
+    with open(os.path.join(CSRC, "batch_kernels.cuh")) as fh:
+        batch = fh.read()
     for dim in (2, 3, 4):
         for real, is_float in (("double", 0), ("float", 1)):
             for pmode in (0, 1, 2):
                 src = (f"#define DP_DIM {dim}\n#define DP_REAL {real}\n#define DP_REAL_IS_FLOAT {is_float}\n"
                        f"#define DP_PMODE {pmode}\n#define DP_SIGMA_ONE {int(pmode == 0)}\n"
                        f"#define DP_EPS_ONE {int(pmode == 0)}\n#include <cstdint>\n"
-                       + common + SAMPLE_POTENTIAL + pair)
+                       + common + SAMPLE_POTENTIAL + pair + (batch if is_float and pmode == 0 else ""))
                 path = os.path.join(BUILD, f"pair_check_{dim}_{real}_{pmode}.cu")
                 with open(path, "w") as fh:
                     fh.write(src)

@@ -116,6 +116,18 @@ _SIGNATURES = {
     "dp_time_kernel": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "dp_time_forces": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "dp_kernel_launches": (ctypes.c_int64, [_P]),
+    "dp_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _I32, ctypes.POINTER(_P)]),
+    "dp_batch_destroy": (ctypes.c_int, [_P]),
+    "dp_batch_set_state": (ctypes.c_int, [_P, _D, _D, _D, _D]),
+    "dp_batch_get_state": (ctypes.c_int, [_P, _D, _D, _I32]),
+    "dp_batch_set_potential": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_double]),
+    "dp_batch_set_integrator": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_uint64]),
+    "dp_batch_set_launch": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "dp_batch_run": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.POINTER(ctypes.c_float)]),
+    "dp_batch_observables": (ctypes.c_int, [_P, _D, ctypes.c_int]),
+    "dp_batch_last_forces": (ctypes.c_int, [_P, _D]),
     "dp_sum_mv2_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_void_p]),
 }

@@ -1,0 +1,250 @@
+// batch_kernels.cuh — thousands of independent replicas in one persistent
+// kernel (compiled by NVRTC together with pair_kernels.cuh and the generated
+// pair potential).
+//
+// Each CTA takes a replica from a work queue (largest first) and runs all
+// `steps` steps of it before taking the next, so replicas never wait on one
+// another. Per step, inside the CTA:
+//   1. cell binning in shared memory: the replica's fixed-point positions
+//      are counting-sorted into cells at least r_cut wide (no skin, no
+//      Verlet list: the cells are rebuilt every step), or kept in index
+//      order when a box has fewer than 3 cells per axis (all-pairs);
+//   2. pair forces in float32 from the fixed-point displacements (27-cell
+//      stencil), the replica's positions read from shared memory;
+//   3. G-JF (or NVE) leap-frog in float64 as dompap/integrator.py:17-40, wrap
+//      as dompap/positions.py:90-98, new fixed-point position to HBM.
+// Every `sample_every` steps the CTA adds U, W and sum m v^2 of the replica to
+// its observable slots (float64).
+
+__device__ __forceinline__ int dp_batch_block_scan(int* cnt, int nc, int* warp_tot) {
+    // exclusive scan of cnt[0..nc) in place, blockDim.x threads; returns the total
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int carry = 0;
+    for (int base = 0; base < nc; base += blockDim.x) {
+        const int c = base + threadIdx.x;
+        const int v = c < nc ? cnt[c] : 0;
+        int x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int w = lane < nw ? warp_tot[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            if (lane < nw) warp_tot[lane] = w;  // inclusive warp totals
+        }
+        __syncthreads();
+        const int before = (warp > 0 ? warp_tot[warp - 1] : 0) + carry;
+        if (c < nc) cnt[c] = before + x - v;
+        carry += warp_tot[nw - 1];
+        __syncthreads();
+    }
+    return carry;
+}
+
+template <int THREADS>
+__device__ __forceinline__ void dp_batch_steps(const dp_batch_args& a) {
+    constexpr int D = DP_DIM;
+    typedef typename dp_shadow_t<D>::type sh_t;
+    extern __shared__ __align__(16) unsigned char dp_smem[];
+    sh_t* s_sh = (sh_t*)dp_smem;                                  // [max_n] positions sorted by cell
+    unsigned short* s_idx = (unsigned short*)(s_sh + a.max_n);     // [max_n] local index of each slot
+    int* s_start = (int*)(s_idx + ((a.max_n + 7) & ~7));           // [max_cells + 1]
+    int* s_cur = s_start + a.max_cells + 1;                        // [max_cells]
+    __shared__ int s_rep;
+    __shared__ int s_warp[32];
+    __shared__ double s_red[32];
+    sh_t* gsh = (sh_t*)a.shadow;
+    const long long ntot = a.ntot;
+
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_rep = atomicAdd(a.queue, 1);
+        __syncthreads();
+        if (s_rep >= a.n_rep) return;
+        const int r = a.order[s_rep];
+        const long long off = a.offset[r];
+        const int n = (int)(a.offset[r + 1] - off);
+        double L[D], scale[D];
+        float unit[D];
+        int nc[D];
+        bool cells = true;
+        int ncell = 1;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            L[k] = a.box[r * DP_MAX_DIM + k];
+            scale[k] = 4294967296.0 / L[k];
+            unit[k] = (float)(L[k] / 4294967296.0);
+            nc[k] = a.ncell[r * DP_MAX_DIM + k];
+            cells = cells && nc[k] >= 3;
+            ncell *= max(nc[k], 1);
+        }
+        double c[5];
+#pragma unroll
+        for (int t = 0; t < 5; ++t) c[t] = a.coef[r * 5 + t];
+
+        const long long step0 = a.st->step;  // advanced by the host-side graph after this launch
+        for (int step = 0; step < a.steps; ++step) {
+            const long long gstep = step0 + step;
+            const bool sample = a.sample_every > 0 && ((gstep + 1) % a.sample_every) == 0;
+            // ---- 1. binning
+            if (cells) {
+                for (int q = threadIdx.x; q < ncell; q += THREADS) s_start[q] = 0;
+                __syncthreads();
+                for (int p = threadIdx.x; p < n; p += THREADS) {
+                    uint32_t u[D];
+                    dp_shadow_unpack<D>(gsh[off + p], u);
+                    int l = 0;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) l = l * nc[k] + (int)__umulhi(u[k], (uint32_t)nc[k]);
+                    atomicAdd(s_start + l, 1);
+                }
+                __syncthreads();
+                dp_batch_block_scan(s_start, ncell, s_warp);
+                for (int q = threadIdx.x; q < ncell; q += THREADS) s_cur[q] = s_start[q];
+                if (threadIdx.x == 0) s_start[ncell] = n;
+                __syncthreads();
+                for (int p = threadIdx.x; p < n; p += THREADS) {
+                    const sh_t v = gsh[off + p];
+                    uint32_t u[D];
+                    dp_shadow_unpack<D>(v, u);
+                    int l = 0;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) l = l * nc[k] + (int)__umulhi(u[k], (uint32_t)nc[k]);
+                    const int slot = atomicAdd(s_cur + l, 1);
+                    s_sh[slot] = v;
+                    s_idx[slot] = (unsigned short)p;
+                }
+            } else {
+                for (int p = threadIdx.x; p < n; p += THREADS) {
+                    s_sh[p] = gsh[off + p];
+                    s_idx[p] = (unsigned short)p;
+                }
+            }
+            __syncthreads();
+            // ---- 2. forces (float32) and 3. integration (float64)
+            double accU = 0.0, accW = 0.0, accK = 0.0;
+            for (int slot = threadIdx.x; slot < n; slot += THREADS) {
+                uint32_t up[D];
+                dp_shadow_unpack<D>(s_sh[slot], up);
+                float f[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) f[k] = 0.0f;
+                float eu = 0.0f, ew = 0.0f;
+                auto pair = [&](int q) {
+                    uint32_t uq[D];
+                    dp_shadow_unpack<D>(s_sh[q], uq);
+                    float df[D];
+                    const float q2 = dp_shadow_q<D>(up, uq, unit, df);
+                    if (q2 <= a.rc2) {
+                        const float rinv = rsqrtf(q2);
+                        const float rr = q2 * rinv;
+                        const float sf = dp_pair_f<float>(rr, rinv);
+                        const float g = sf * rinv;
+#pragma unroll
+                        for (int k = 0; k < D; ++k) f[k] = fmaf(g, df[k], f[k]);
+                        if (sample) {
+                            eu += dp_pair_u<float>(rr, rinv);
+                            ew += sf * rr;
+                        }
+                    }
+                };
+                if (cells) {
+                    int cp[D];
+#pragma unroll
+                    for (int k = 0; k < D; ++k) cp[k] = (int)__umulhi(up[k], (uint32_t)nc[k]);
+                    int stencil = 1;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) stencil *= 3;
+                    for (int s = 0; s < stencil; ++s) {
+                        int rem = s, l = 0;
+#pragma unroll
+                        for (int k = 0; k < D; ++k) {
+                            int cc = cp[k] + (rem % 3) - 1;
+                            rem /= 3;
+                            cc += (cc < 0) ? nc[k] : 0;
+                            cc -= (cc >= nc[k]) ? nc[k] : 0;
+                            l = l * nc[k] + cc;
+                        }
+                        const int e = s_start[l + 1];
+                        for (int q = s_start[l]; q < e; ++q)
+                            if (q != slot) pair(q);
+                    }
+                } else {
+                    for (int q = 0; q < n; ++q)
+                        if (q != slot) pair(q);
+                }
+                // integrate particle i (float64)
+                const long long i = off + s_idx[slot];
+                float z[4];
+                if (!a.nve) dp_normals4(a.seed, (unsigned long long)gstep, (uint32_t)i, z);
+                uint32_t un[D];
+                double ke = 0.0;
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    const long long o = k * ntot + i;
+                    double v = a.vel[o];
+                    double x = a.pos[o];
+                    const double F = (double)f[k];
+                    if (a.nve) {
+                        v = v + c[4] * F;
+                    } else {
+                        const double bn = c[3] * (double)z[k];
+                        v = c[0] * v + c[1] * F + c[2] * (a.beta[o] + bn);
+                        a.beta[o] = bn;
+                    }
+                    x = x + v * a.dt;
+                    const long long t = __double2ll_rd(x * scale[k]);
+                    if (t < 0 || t >= 4294967296LL) {
+                        if (!(x >= 0.0 && x < L[k])) {
+                            const double sh = floor(x / L[k]);
+                            a.img[o] += (int32_t)sh;
+                            x -= sh * L[k];
+                        }
+                        un[k] = dp_fixed(x, scale[k]);
+                        if (!isfinite(x)) atomicExch(&a.st->nonfinite, 1);
+                    } else {
+                        un[k] = (uint32_t)t;
+                    }
+                    a.vel[o] = v;
+                    a.pos[o] = x;
+                    ke += v * v;
+                    if (a.force_out) a.force_out[o] = f[k];
+                }
+                gsh[i] = dp_shadow_pack<D>(un);
+                if (sample) {
+                    accU += (double)eu;
+                    accW += (double)ew;
+                    accK += ke / c[4] * a.dt;  // m |v|^2 with m = dt / (dt/m)
+                }
+            }
+            __syncthreads();
+            if (sample) {
+                const double U = dp_block_sum(accU, s_red);
+                __syncthreads();
+                const double W = dp_block_sum(accW, s_red);
+                __syncthreads();
+                const double K = dp_block_sum(accK, s_red);
+                if (threadIdx.x == 0) {
+                    a.obs[r * 4 + 0] += 0.5 * U;
+                    a.obs[r * 4 + 1] += 0.5 * W / D;
+                    a.obs[r * 4 + 2] += K;
+                    a.obs[r * 4 + 3] += 1.0;
+                }
+                __syncthreads();
+            }
+        }
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(128) dp_batch_steps_128(dp_batch_args a) { dp_batch_steps<128>(a); }
+extern "C" __global__ void __launch_bounds__(256) dp_batch_steps_256(dp_batch_args a) { dp_batch_steps<256>(a); }
+extern "C" __global__ void __launch_bounds__(512) dp_batch_steps_512(dp_batch_args a) { dp_batch_steps<512>(a); }
+extern "C" __global__ void __launch_bounds__(1024) dp_batch_steps_1024(dp_batch_args a) { dp_batch_steps<1024>(a); }

@@ -763,6 +763,7 @@ static double* g_noalloc_addr[64] = {nullptr};
 struct PairLib {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t forces = nullptr, energy = nullptr, virial = nullptr, laplacian = nullptr, eval = nullptr;
+    cudaKernel_t batch[4] = {nullptr, nullptr, nullptr, nullptr};  // 128, 256, 512, 1024 threads
 };
 
 static std::mutex g_lib_mutex;
@@ -801,6 +802,12 @@ static int compile_pair_lib(const std::string& src, PairLib* out) {
     CK(cudaLibraryGetKernel(&pl.virial, pl.lib, "dp_virial"));
     CK(cudaLibraryGetKernel(&pl.laplacian, pl.lib, "dp_laplacian"));
     CK(cudaLibraryGetKernel(&pl.eval, pl.lib, "dp_eval_pair"));
+    if (src.find("dp_batch_steps_128") != std::string::npos) {
+        CK(cudaLibraryGetKernel(&pl.batch[0], pl.lib, "dp_batch_steps_128"));
+        CK(cudaLibraryGetKernel(&pl.batch[1], pl.lib, "dp_batch_steps_256"));
+        CK(cudaLibraryGetKernel(&pl.batch[2], pl.lib, "dp_batch_steps_512"));
+        CK(cudaLibraryGetKernel(&pl.batch[3], pl.lib, "dp_batch_steps_1024"));
+    }
     g_libs.emplace(src, pl);
     *out = pl;
     return DP_OK;
@@ -1686,24 +1693,34 @@ static std::string hexd(double v) {
     return buf;
 }
 
-static int rebuild_pair_lib(dp_sim* s) {
+static std::string pair_program(int dim, int precision, int pmode, bool sig_one, bool eps_one,
+                                const std::string& pot_src, bool with_batch) {
     std::string src;
-    src += "#define DP_DIM " + std::to_string(s->dim) + "\n";
-    if (s->precision == DP_PREC_FP32) {
+    src += "#define DP_DIM " + std::to_string(dim) + "\n";
+    if (precision == DP_PREC_FP32) {
         src += "#define DP_REAL float\n#define DP_REAL_IS_FLOAT 1\n";
     } else {
         src += "#define DP_REAL double\n#define DP_REAL_IS_FLOAT 0\n";
     }
-    src += "#define DP_PMODE " + std::to_string(s->pmode) + "\n";
-    const bool sig_one = s->pmode == DP_PAIR_CONST && s->sigma == 1.0;
-    const bool eps_one = s->pmode == DP_PAIR_CONST && s->epsilon == 1.0;
+    src += "#define DP_PMODE " + std::to_string(pmode) + "\n";
     src += std::string("#define DP_SIGMA_ONE ") + (sig_one ? "1" : "0") + "\n";
     src += std::string("#define DP_EPS_ONE ") + (eps_one ? "1" : "0") + "\n";
     src += dp_src_common;
     src += "\n// ---- generated pair potential ----\n";
-    src += s->pot_src;
+    src += pot_src;
     src += "\n// ---- pair kernels ----\n";
     src += dp_src_pair;
+    if (with_batch) {
+        src += "\n// ---- batched replicas ----\n";
+        src += dp_src_batch;
+    }
+    return src;
+}
+
+static int rebuild_pair_lib(dp_sim* s) {
+    const bool sig_one = s->pmode == DP_PAIR_CONST && s->sigma == 1.0;
+    const bool eps_one = s->pmode == DP_PAIR_CONST && s->epsilon == 1.0;
+    const std::string src = pair_program(s->dim, s->precision, s->pmode, sig_one, eps_one, s->pot_src, false);
     PairLib pl;
     RET(compile_pair_lib(src, &pl));
     s->lib = pl;
@@ -2095,5 +2112,441 @@ int dp_sum_mv2_noalloc(const double* velocities, const double* masses, int64_t n
 }
 
 int64_t dp_kernel_launches(dp_sim* s) { return s ? s->launches_last : 0; }
+
+}  // extern "C"
+
+// ===========================================================================
+// batched replicas (many independent small systems, one persistent kernel)
+// ===========================================================================
+namespace {
+
+// Fixed-point shadow of every particle of every replica (each with its box).
+__global__ void k_batch_shadow(const double* pos, void* shadow, const int32_t* rep_of, const double* box, int dim,
+                               long long ntot) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntot) return;
+    const int r = rep_of[i];
+    uint32_t u[DP_MAX_DIM] = {0, 0, 0, 0};
+    for (int k = 0; k < dim; ++k) u[k] = dp_fixed(pos[k * ntot + i], 4294967296.0 / box[r * DP_MAX_DIM + k]);
+    if (dim == 2)
+        ((uint2*)shadow)[i] = make_uint2(u[0], u[1]);
+    else
+        ((uint4*)shadow)[i] = make_uint4(u[0], u[1], u[2], u[3]);
+}
+
+}  // namespace
+
+struct BatchGraph {
+    long long steps;
+    int sample_every, nve, record;
+    unsigned long long version;
+    cudaGraphExec_t exec;
+};
+
+struct dp_batch {
+    int dim = 3;
+    int n_rep = 0;
+    long long ntot = 0;
+    cudaStream_t stream = nullptr, stream2 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, fork = nullptr, join = nullptr;
+    double *pos = nullptr, *vel = nullptr, *beta = nullptr, *stage = nullptr;
+    int32_t *img = nullptr, *rep_of = nullptr, *order = nullptr, *ncell = nullptr, *queue = nullptr;
+    void* shadow = nullptr;
+    long long* offset = nullptr;
+    double *box = nullptr, *coef = nullptr, *obs = nullptr;
+    float* force_out = nullptr;
+    dp_dev_status* dstat = nullptr;
+    dp_dev_status* hstat = nullptr;
+    std::vector<long long> h_offset;
+    std::vector<double> h_box, h_temp;
+    std::vector<int> h_ncell, h_order;
+    bool have_state = false, have_pot = false;
+    std::string pot_src;
+    double r_cut = 2.5;
+    PairLib lib;
+    double dt = 0.005, tau = 0.1, mass = 1.0;
+    unsigned long long seed = 0;
+    int split_n = 1024, threads_small = 256, threads_large = 1024;
+    unsigned long long version = 1;
+    std::vector<BatchGraph> graphs;
+};
+
+static int batch_kernel_index(int threads) {
+    switch (threads) {
+        case 128: return 0;
+        case 256: return 1;
+        case 512: return 2;
+        case 1024: return 3;
+        default: return -1;
+    }
+}
+
+static int batch_upload_coef(dp_batch* b) {
+    std::vector<double> coef((size_t)b->n_rep * 5);
+    const double m = b->mass;
+    for (int r = 0; r < b->n_rep; ++r) {
+        const double T = b->h_temp.empty() ? 1.0 : b->h_temp[r];
+        const double alpha = m / b->tau;  // dompap/integrator.py:29-36
+        const double beta_variance = 2 * alpha * T * b->dt;
+        const double numerator = 1.0 - alpha * b->dt / 2.0 / m;
+        const double denominator = 1.0 + alpha * b->dt / 2.0 / m;
+        const double bb = 1 / denominator;
+        coef[r * 5 + 0] = numerator / denominator;
+        coef[r * 5 + 1] = bb * b->dt / m;
+        coef[r * 5 + 2] = bb / 2 / m;
+        coef[r * 5 + 3] = std::sqrt(beta_variance);
+        coef[r * 5 + 4] = b->dt / m;
+    }
+    CK(cudaMemcpy(b->coef, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice));
+    b->version++;
+    return DP_OK;
+}
+
+static int batch_configure_cells(dp_batch* b) {
+    b->h_ncell.assign((size_t)b->n_rep * DP_MAX_DIM, 0);
+    for (int r = 0; r < b->n_rep; ++r) {
+        bool ok = true;
+        int nc[DP_MAX_DIM] = {0, 0, 0, 0};
+        for (int k = 0; k < b->dim; ++k) {
+            nc[k] = (int)std::floor(b->h_box[r * DP_MAX_DIM + k] / (b->r_cut * (1.0 + 1e-6)));
+            ok = ok && nc[k] >= 3;
+        }
+        long long cells = 1;
+        for (int k = 0; k < b->dim; ++k) cells *= std::max(nc[k], 1);
+        if (!ok || cells > 32768) continue;  // all pairs inside the replica
+        for (int k = 0; k < b->dim; ++k) b->h_ncell[r * DP_MAX_DIM + k] = nc[k];
+    }
+    CK(cudaMemcpy(b->ncell, b->h_ncell.data(), b->h_ncell.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    b->version++;
+    return DP_OK;
+}
+
+// Replicas sorted by size (largest first) and split into a small and a large
+// bucket, each run by its own persistent launch.
+struct BatchBucket {
+    int first, count, threads, max_n, max_cells;
+};
+
+static void batch_buckets(const dp_batch* b, BatchBucket* out, int* nb) {
+    *nb = 0;
+    int large = 0;
+    while (large < b->n_rep) {
+        const int r = b->h_order[large];
+        if (b->h_offset[r + 1] - b->h_offset[r] <= b->split_n) break;
+        ++large;
+    }
+    auto fill = [&](int first, int count, int threads) {
+        BatchBucket bk{first, count, threads, 0, 1};
+        for (int q = first; q < first + count; ++q) {
+            const int r = b->h_order[q];
+            bk.max_n = std::max(bk.max_n, (int)(b->h_offset[r + 1] - b->h_offset[r]));
+            int cells = 1;
+            for (int k = 0; k < b->dim; ++k) cells *= std::max(b->h_ncell[r * DP_MAX_DIM + k], 1);
+            bk.max_cells = std::max(bk.max_cells, cells);
+        }
+        out[(*nb)++] = bk;
+    };
+    if (large > 0) fill(0, large, b->threads_large);
+    if (large < b->n_rep) fill(large, b->n_rep - large, b->threads_small);
+}
+
+static size_t batch_smem(int dim, int max_n, int max_cells) {
+    const size_t sh = (dim == 2 ? 8 : 16);
+    return (size_t)max_n * sh + (size_t)((max_n + 7) & ~7) * 2 + (size_t)(2 * max_cells + 1) * 4;
+}
+
+static int batch_record(dp_batch* b, long long steps, int sample_every, int nve, int record) {
+    BatchBucket bk[2];
+    int nb = 0;
+    batch_buckets(b, bk, &nb);
+    CK(cudaMemsetAsync(b->queue, 0, 2 * sizeof(int32_t), b->stream));
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (nb == 2) {
+        CK(cudaEventRecord(b->fork, b->stream));
+        CK(cudaStreamWaitEvent(b->stream2, b->fork, 0));
+    }
+    for (int q = 0; q < nb; ++q) {
+        const BatchBucket& k = bk[q];
+        const int ki = batch_kernel_index(k.threads);
+        if (ki < 0) return fail(DP_ERR_ARG, "threads per replica must be 128, 256, 512 or 1024");
+        if (k.max_n > 65535) return fail(DP_ERR_ARG, "a replica has more than 65535 particles");
+        const size_t smem = batch_smem(b->dim, k.max_n, k.max_cells);
+        if (smem > 227 * 1024)
+            return fail(DP_ERR_ARG, "a replica does not fit in shared memory (" + std::to_string(smem) + " bytes)");
+        CK(cudaKernelSetAttributeForDevice(b->lib.batch[ki], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem,
+                                           dev));
+        dp_batch_args a;
+        memset(&a, 0, sizeof(a));
+        a.pos = b->pos;
+        a.vel = b->vel;
+        a.beta = b->beta;
+        a.img = b->img;
+        a.shadow = b->shadow;
+        a.offset = b->offset;
+        a.order = b->order + k.first;
+        a.box = b->box;
+        a.coef = b->coef;
+        a.ncell = b->ncell;
+        a.obs = b->obs;
+        a.force_out = record ? b->force_out : nullptr;
+        a.queue = b->queue + q;
+        a.st = b->dstat;
+        a.ntot = b->ntot;
+        a.n_rep = k.count;
+        a.steps = (int)steps;
+        a.sample_every = sample_every;
+        a.max_n = k.max_n;
+        a.max_cells = k.max_cells;
+        a.nve = nve;
+        a.dt = b->dt;
+        a.rc2 = (float)(b->r_cut * b->r_cut);
+        a.seed = b->seed;
+        const int per_sm = std::max(1, std::min(2048 / k.threads, (int)((228 * 1024) / (smem + 1024))));
+        const unsigned grid = (unsigned)std::max(1, std::min(k.count, sms * per_sm));
+        void* args[] = {&a};
+        cudaStream_t st = (q == 0) ? b->stream : b->stream2;
+        CK(cudaLaunchKernel((const void*)b->lib.batch[ki], dim3(grid), dim3(k.threads), args, smem, st));
+    }
+    if (nb == 2) {
+        CK(cudaEventRecord(b->join, b->stream2));
+        CK(cudaStreamWaitEvent(b->stream, b->join, 0));
+    }
+    k_advance_step<<<1, 1, 0, b->stream>>>(b->dstat, steps);
+    CK(cudaGetLastError());
+    return DP_OK;
+}
+
+extern "C" {
+
+int dp_batch_create(int dim, int n_rep, const int32_t* counts, dp_batch** out) {
+    if (!out || !counts) return fail(DP_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (dim < 2 || dim > 4) return fail(DP_ERR_ARG, "dimension must be 2, 3 or 4");
+    if (n_rep < 1) return fail(DP_ERR_ARG, "need at least one replica");
+    dp_batch* b = new dp_batch();
+    b->dim = dim;
+    b->n_rep = n_rep;
+    b->h_offset.assign((size_t)n_rep + 1, 0);
+    for (int r = 0; r < n_rep; ++r) {
+        if (counts[r] < 2 || counts[r] > 65535) {
+            delete b;
+            return fail(DP_ERR_ARG, "replica sizes must be in [2, 65535]");
+        }
+        b->h_offset[r + 1] = b->h_offset[r] + counts[r];
+    }
+    b->ntot = b->h_offset[n_rep];
+    b->h_order.resize(n_rep);
+    for (int r = 0; r < n_rep; ++r) b->h_order[r] = r;
+    std::stable_sort(b->h_order.begin(), b->h_order.end(), [&](int x, int y) { return counts[x] > counts[y]; });
+    int rc = DP_OK;
+    auto cleanup = [&]() {
+        dp_batch_destroy(b);
+        return rc;
+    };
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess) {
+        rc = fail(DP_ERR_CUDA, "stream/event creation failed");
+        return cleanup();
+    }
+    const size_t nd = (size_t)b->ntot * dim;
+    if ((rc = dalloc_t(&b->pos, nd)) || (rc = dalloc_t(&b->vel, nd)) || (rc = dalloc_t(&b->beta, nd)) ||
+        (rc = dalloc_t(&b->stage, nd)) || (rc = dalloc_t(&b->img, nd)) || (rc = dalloc_t(&b->rep_of, b->ntot)) ||
+        (rc = dalloc_t(&b->order, (size_t)n_rep)) || (rc = dalloc_t(&b->ncell, (size_t)n_rep * DP_MAX_DIM)) ||
+        (rc = dalloc_t(&b->queue, 2)) || (rc = dalloc_t(&b->offset, (size_t)n_rep + 1)) ||
+        (rc = dalloc_t(&b->box, (size_t)n_rep * DP_MAX_DIM)) || (rc = dalloc_t(&b->coef, (size_t)n_rep * 5)) ||
+        (rc = dalloc_t(&b->obs, (size_t)n_rep * 4)) || (rc = dalloc(&b->shadow, (size_t)b->ntot * (dim == 2 ? 8 : 16))))
+        return cleanup();
+    if (cudaMalloc(&b->dstat, sizeof(dp_dev_status)) != cudaSuccess ||
+        cudaMallocHost(&b->hstat, sizeof(dp_dev_status)) != cudaSuccess) {
+        rc = fail(DP_ERR_CUDA, "status allocation failed");
+        return cleanup();
+    }
+    memset(b->hstat, 0, sizeof(dp_dev_status));
+    std::vector<int32_t> rep_of((size_t)b->ntot);
+    for (int r = 0; r < n_rep; ++r)
+        for (long long i = b->h_offset[r]; i < b->h_offset[r + 1]; ++i) rep_of[i] = r;
+    if (cudaMemcpy(b->dstat, b->hstat, sizeof(dp_dev_status), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b->rep_of, rep_of.data(), rep_of.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b->offset, b->h_offset.data(), b->h_offset.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b->order, b->h_order.data(), (size_t)n_rep * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(b->obs, 0, (size_t)n_rep * 4 * 8) != cudaSuccess || cudaMemset(b->img, 0, nd * 4) != cudaSuccess ||
+        cudaMemset(b->beta, 0, nd * 8) != cudaSuccess) {
+        rc = fail(DP_ERR_CUDA, "batch initialisation failed");
+        return cleanup();
+    }
+    *out = b;
+    return DP_OK;
+}
+
+int dp_batch_destroy(dp_batch* b) {
+    if (!b) return DP_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->stream2) cudaStreamSynchronize(b->stream2);
+    for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+    void* bufs[] = {b->pos, b->vel, b->beta, b->stage, b->img, b->rep_of, b->order, b->ncell, b->queue, b->shadow,
+                    b->offset, b->box, b->coef, b->obs, b->force_out, b->dstat};
+    for (void* p : bufs)
+        if (p) cudaFree(p);
+    if (b->hstat) cudaFreeHost(b->hstat);
+    cudaEvent_t evs[] = {b->ev0, b->ev1, b->fork, b->join};
+    for (cudaEvent_t e : evs)
+        if (e) cudaEventDestroy(e);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->stream2) cudaStreamDestroy(b->stream2);
+    delete b;
+    return DP_OK;
+}
+
+int dp_batch_set_state(dp_batch* b, const double* positions, const double* velocities, const double* boxes,
+                       const double* temperatures) {
+    if (!b || !positions || !velocities || !boxes || !temperatures) return fail(DP_ERR_ARG, "null argument");
+    b->h_box.assign((size_t)b->n_rep * DP_MAX_DIM, 1.0);
+    b->h_temp.assign(temperatures, temperatures + b->n_rep);
+    for (int r = 0; r < b->n_rep; ++r)
+        for (int k = 0; k < b->dim; ++k) {
+            const double L = boxes[r * b->dim + k];
+            if (!(L > 0.0) || !std::isfinite(L)) return fail(DP_ERR_ARG, "box sides must be positive");
+            b->h_box[r * DP_MAX_DIM + k] = L;
+        }
+    const size_t bytes = (size_t)b->ntot * b->dim * sizeof(double);
+    CK(cudaMemcpy(b->box, b->h_box.data(), b->h_box.size() * 8, cudaMemcpyHostToDevice));
+    const unsigned g = grid_for(b->ntot * b->dim, kBlock);
+    CK(cudaMemcpyAsync(b->stage, positions, bytes, cudaMemcpyHostToDevice, b->stream));
+    k_aos_to_soa_f64<<<g, kBlock, 0, b->stream>>>(b->stage, b->pos, b->ntot, b->dim);
+    CK(cudaMemcpyAsync(b->stage, velocities, bytes, cudaMemcpyHostToDevice, b->stream));
+    k_aos_to_soa_f64<<<g, kBlock, 0, b->stream>>>(b->stage, b->vel, b->ntot, b->dim);
+    k_batch_shadow<<<grid_for(b->ntot, kBlock), kBlock, 0, b->stream>>>(b->pos, b->shadow, b->rep_of, b->box, b->dim,
+                                                                        b->ntot);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(b->stream));
+    b->have_state = true;
+    if (b->have_pot) RET(batch_configure_cells(b));
+    return batch_upload_coef(b);
+}
+
+int dp_batch_get_state(dp_batch* b, double* positions, double* velocities, int32_t* images) {
+    if (!b) return fail(DP_ERR_ARG, "null handle");
+    const size_t bytes = (size_t)b->ntot * b->dim * sizeof(double);
+    const unsigned g = grid_for(b->ntot * b->dim, kBlock);
+    if (positions) {
+        k_soa_to_aos_f64<<<g, kBlock, 0, b->stream>>>(b->pos, b->stage, b->ntot, b->dim);
+        CK(cudaMemcpyAsync(positions, b->stage, bytes, cudaMemcpyDeviceToHost, b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+    }
+    if (velocities) {
+        k_soa_to_aos_f64<<<g, kBlock, 0, b->stream>>>(b->vel, b->stage, b->ntot, b->dim);
+        CK(cudaMemcpyAsync(velocities, b->stage, bytes, cudaMemcpyDeviceToHost, b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+    }
+    if (images) {
+        int32_t* st = (int32_t*)b->stage;
+        k_soa_to_aos_i32<<<g, kBlock, 0, b->stream>>>(b->img, st, b->ntot, b->dim);
+        CK(cudaMemcpyAsync(images, st, (size_t)b->ntot * b->dim * 4, cudaMemcpyDeviceToHost, b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+    }
+    CK(cudaGetLastError());
+    return DP_OK;
+}
+
+int dp_batch_set_potential(dp_batch* b, const char* device_source, double r_cut) {
+    if (!b || !device_source) return fail(DP_ERR_ARG, "null argument");
+    if (!(r_cut > 0.0) || !std::isfinite(r_cut)) return fail(DP_ERR_ARG, "r_cut must be positive and finite");
+    const std::string src = pair_program(b->dim, DP_PREC_FP32, DP_PAIR_CONST, true, true, device_source, true);
+    PairLib pl;
+    RET(compile_pair_lib(src, &pl));
+    if (!pl.batch[0]) return fail(DP_ERR_NVRTC, "batch kernels missing from the compiled program");
+    b->lib = pl;
+    b->pot_src = device_source;
+    b->r_cut = r_cut;
+    b->have_pot = true;
+    b->version++;
+    if (b->have_state) RET(batch_configure_cells(b));
+    return DP_OK;
+}
+
+int dp_batch_set_integrator(dp_batch* b, double time_step, double damping_time, double mass, uint64_t seed) {
+    if (!b) return fail(DP_ERR_ARG, "null handle");
+    if (!(mass > 0.0)) return fail(DP_ERR_ARG, "mass must be positive");
+    b->dt = time_step;
+    b->tau = damping_time;
+    b->mass = mass;
+    b->seed = seed;
+    return batch_upload_coef(b);
+}
+
+int dp_batch_set_launch(dp_batch* b, int split_n, int threads_small, int threads_large) {
+    if (!b) return fail(DP_ERR_ARG, "null handle");
+    if (batch_kernel_index(threads_small) < 0 || batch_kernel_index(threads_large) < 0)
+        return fail(DP_ERR_ARG, "threads per replica must be 128, 256, 512 or 1024");
+    b->split_n = std::max(0, split_n);
+    b->threads_small = threads_small;
+    b->threads_large = threads_large;
+    b->version++;
+    return DP_OK;
+}
+
+int dp_batch_run(dp_batch* b, int64_t steps, int sample_every, int nve, int record_forces, float* ms) {
+    if (!b) return fail(DP_ERR_ARG, "null handle");
+    if (!b->have_state || !b->have_pot) return fail(DP_ERR_NOPOT, "batch state or potential not set");
+    if (steps < 0 || steps > (1LL << 30)) return fail(DP_ERR_ARG, "bad step count");
+    if (steps == 0) return DP_OK;
+    if (record_forces && !b->force_out) RET(dalloc_t(&b->force_out, (size_t)b->ntot * b->dim));
+    BatchGraph* g = nullptr;
+    for (auto& x : b->graphs)
+        if (x.steps == steps && x.sample_every == sample_every && x.nve == nve && x.record == record_forces &&
+            x.version == b->version)
+            g = &x;
+    if (!g) {
+        for (auto& x : b->graphs) cudaGraphExecDestroy(x.exec);
+        b->graphs.clear();
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = batch_record(b, steps, sample_every, nve, record_forces);
+        const cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+        if (rc != DP_OK) return rc;
+        if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+        BatchGraph bg{steps, sample_every, nve, record_forces, b->version, nullptr};
+        const cudaError_t ei = cudaGraphInstantiate(&bg.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) return fail(DP_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ei));
+        b->graphs.push_back(bg);
+        g = &b->graphs.back();
+    }
+    if (ms) CK(cudaEventRecord(b->ev0, b->stream));
+    CK(cudaGraphLaunch(g->exec, b->stream));
+    if (ms) CK(cudaEventRecord(b->ev1, b->stream));
+    CK(cudaMemcpyAsync(b->hstat, b->dstat, sizeof(dp_dev_status), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    if (ms) CK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
+    if (b->hstat->nonfinite) {
+        b->hstat->nonfinite = 0;
+        CK(cudaMemcpy(b->dstat, b->hstat, sizeof(dp_dev_status), cudaMemcpyHostToDevice));
+        return fail(DP_ERR_NONFINITE, "a position became NaN/Inf in a replica");
+    }
+    return DP_OK;
+}
+
+int dp_batch_observables(dp_batch* b, double* out, int reset) {
+    if (!b || !out) return fail(DP_ERR_ARG, "null argument");
+    CK(cudaMemcpy(out, b->obs, (size_t)b->n_rep * 4 * sizeof(double), cudaMemcpyDeviceToHost));
+    if (reset) CK(cudaMemset(b->obs, 0, (size_t)b->n_rep * 4 * sizeof(double)));
+    return DP_OK;
+}
+
+int dp_batch_last_forces(dp_batch* b, double* forces) {
+    if (!b || !forces) return fail(DP_ERR_ARG, "null argument");
+    if (!b->force_out) return fail(DP_ERR_ARG, "no step was run with record_forces");
+    std::vector<float> f((size_t)b->ntot * b->dim);
+    CK(cudaMemcpy(f.data(), b->force_out, f.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (long long i = 0; i < b->ntot; ++i)
+        for (int k = 0; k < b->dim; ++k) forces[i * b->dim + k] = (double)f[(size_t)k * b->ntot + i];
+    return DP_OK;
+}
 
 }  // extern "C"

@@ -55,6 +55,35 @@ struct dp_pair_args {
     int pad1;
 };
 
+// Arguments of the batched-replica kernel (batch_kernels.cuh).
+struct dp_batch_args {
+    double* pos;               // SoA [k * ntot + i]
+    double* vel;
+    double* beta;
+    int32_t* img;
+    void* shadow;              // fixed-point positions, one vector per particle
+    const long long* offset;   // [n_rep + 1] first particle of each replica
+    const int32_t* order;      // replicas in processing order (this launch's bucket)
+    const double* box;         // [n_rep * DP_MAX_DIM]
+    const double* coef;        // [n_rep * 5] G-JF a, b dt/m, b/(2m), sqrt(2 alpha T dt), dt/m
+    const int32_t* ncell;      // [n_rep * DP_MAX_DIM] cells per axis, 0 = all pairs
+    double* obs;               // [n_rep * 4] sum U, sum W, sum m v^2, samples
+    float* force_out;          // optional SoA float forces of the last step
+    int32_t* queue;            // work counter of this launch (zeroed before it)
+    dp_dev_status* st;
+    long long ntot;
+    int n_rep;                 // replicas in `order`
+    int steps;
+    int sample_every;          // accumulate observables every this many steps (0: never)
+    int max_n;                 // shared-memory capacity in particles
+    int max_cells;             // shared-memory capacity in cells
+    int nve;                   // 1: NVE leap-frog instead of G-JF
+    double dt;
+    float rc2;                 // r_cut^2 (float32 cut)
+    int pad;
+    unsigned long long seed;
+};
+
 // ---------------------------------------------------------------------------
 // Minimum image, single +-L shift per axis, exactly as
 // dompap/positions.py:12-16 (box/2 is exact in binary floating point).

@@ -189,6 +189,41 @@ int dp_sum_mv2_noalloc(const double *velocities, const double *masses, int64_t n
 /* Number of kernels the last dp_run launched (graph nodes included). */
 int64_t dp_kernel_launches(dp_sim *sim);
 
+/* ---------------------------------------------------------------------------
+ * Batched replicas: many independent periodic systems (sizes up to 65535,
+ * each with its own box and temperature) advanced by one persistent kernel
+ * per run (captured in a CUDA graph); float32 pair forces from fixed-point
+ * displacements, float64 G-JF / NVE integration and wrap. sigma = epsilon = 1.
+ * Replaces a Python loop of Simulation.run over replicas
+ * (dompap/Simulation.py:726-737 per replica).
+ * ------------------------------------------------------------------------- */
+typedef struct dp_batch dp_batch;
+/* counts: (n_rep,) particles per replica; particles are stored replica after replica. */
+int dp_batch_create(int dim, int n_rep, const int32_t *counts, dp_batch **out);
+int dp_batch_destroy(dp_batch *batch);
+/* positions, velocities: (sum N, D) row-major; boxes: (n_rep, D); temperatures: (n_rep,).
+ * Positions must lie in [0, L) of their replica. */
+int dp_batch_set_state(dp_batch *batch, const double *positions, const double *velocities, const double *boxes,
+                       const double *temperatures);
+/* Any of the outputs may be NULL. images: (sum N, D) int32. */
+int dp_batch_get_state(dp_batch *batch, double *positions, double *velocities, int32_t *images);
+/* Generated pair potential (as dp_set_potential), compiled for the batch kernel. */
+int dp_batch_set_potential(dp_batch *batch, const char *device_source, double r_cut);
+int dp_batch_set_integrator(dp_batch *batch, double time_step, double damping_time, double mass, uint64_t seed);
+/* Replicas with more than split_n particles run with threads_large threads per
+ * CTA, the others with threads_small (128, 256, 512 or 1024): the tile shape
+ * the autotuner picks. */
+int dp_batch_set_launch(dp_batch *batch, int split_n, int threads_small, int threads_large);
+/* `steps` steps of every replica (nve: leap-frog instead of G-JF). Every
+ * sample_every steps (0: never) U, W and sum m v^2 of each replica are added
+ * to its observables. record_forces keeps the last step's float32 forces.
+ * ms (may be NULL) receives the device time. */
+int dp_batch_run(dp_batch *batch, int64_t steps, int sample_every, int nve, int record_forces, float *ms);
+/* (n_rep, 4): sum of U, sum of W, sum of sum m v^2, number of samples. reset != 0 zeroes them. */
+int dp_batch_observables(dp_batch *batch, double *out, int reset);
+/* (sum N, D) forces of the last recorded step (float32 values). */
+int dp_batch_last_forces(dp_batch *batch, double *forces);
+
 #ifdef __cplusplus
 }
 #endif
