@@ -41,7 +41,7 @@ def write_embedded() -> str:
     os.makedirs(BUILD, exist_ok=True)
     parts = []
     for name, sym in (("dp_common.cuh", "dp_src_common"), ("pair_kernels.cuh", "dp_src_pair"),
-                      ("batch_kernels.cuh", "dp_src_batch")):
+                      ("batch_kernels.cuh", "dp_src_batch"), ("mlp_common.cuh", "dp_src_mlp")):
         with open(os.path.join(CSRC, name)) as fh:
             text = fh.read()
         if ')DPSRC"' in text:

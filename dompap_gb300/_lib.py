@@ -26,6 +26,7 @@ DP_ERR_NOPOT = 7
 
 DP_PREC_FP64 = 0
 DP_PREC_FP32 = 1
+DP_PREC_MLP = 2
 DP_NL_CELL = 0
 DP_NL_ALLPAIRS = 1
 DP_INT_GJF = 0
@@ -128,6 +129,21 @@ _SIGNATURES = {
                                     ctypes.POINTER(ctypes.c_float)]),
     "dp_batch_observables": (ctypes.c_int, [_P, _D, ctypes.c_int]),
     "dp_batch_last_forces": (ctypes.c_int, [_P, _D]),
+    "dp_mlp_create": (ctypes.c_int, [ctypes.POINTER(_P)]),
+    "dp_mlp_destroy": (ctypes.c_int, [_P]),
+    "dp_mlp_param_count": (ctypes.c_int, []),
+    "dp_mlp_set_params": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "dp_mlp_get_params": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float)]),
+    "dp_mlp_set_data": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                       ctypes.c_int64]),
+    "dp_mlp_train": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                    ctypes.c_float, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
+    "dp_mlp_eval": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float), ctypes.c_int64,
+                                   ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
+    "dp_mlp_gradients": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                        ctypes.c_int64, ctypes.c_float, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                                        ctypes.POINTER(ctypes.c_float)]),
+    "dp_set_mlp": (ctypes.c_int, [_P, _P]),
     "dp_sum_mv2_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_void_p]),
 }
@@ -172,6 +188,11 @@ def check(rc: int) -> None:
 def dptr(a: np.ndarray):
     assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"], (a.dtype, a.flags)
     return a.ctypes.data_as(_D)
+
+
+def fptr(a: np.ndarray):
+    assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"], (a.dtype, a.flags)
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
 def iptr(a: np.ndarray):

@@ -16,6 +16,7 @@
 //    graph needs no host decision. After each chunk the host reads the status
 //    word; on a neighbour-list or cell overflow it restores the chunk's start
 //    state, grows the capacity and replays the chunk.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <nvrtc.h>
 
@@ -31,7 +32,9 @@
 
 #include "dompap_gpu.h"
 #include "dp_common.cuh"
-#include "dp_embedded.h"  // dp_src_common[], dp_src_pair[] (generated at build time)
+#include "dp_embedded.h"
+#include "mlp_common.cuh"
+#include "mlp_train.cuh"  // dp_src_common[], dp_src_pair[] (generated at build time)
 
 // ===========================================================================
 // errors
@@ -764,6 +767,7 @@ struct PairLib {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t forces = nullptr, energy = nullptr, virial = nullptr, laplacian = nullptr, eval = nullptr;
     cudaKernel_t batch[4] = {nullptr, nullptr, nullptr, nullptr};  // 128, 256, 512, 1024 threads
+    cudaKernel_t forces_mlp = nullptr, energy_mlp = nullptr, virial_mlp = nullptr;
 };
 
 static std::mutex g_lib_mutex;
@@ -802,6 +806,11 @@ static int compile_pair_lib(const std::string& src, PairLib* out) {
     CK(cudaLibraryGetKernel(&pl.virial, pl.lib, "dp_virial"));
     CK(cudaLibraryGetKernel(&pl.laplacian, pl.lib, "dp_laplacian"));
     CK(cudaLibraryGetKernel(&pl.eval, pl.lib, "dp_eval_pair"));
+    if (src.find("#define DP_MLP 1") != std::string::npos) {
+        CK(cudaLibraryGetKernel(&pl.forces_mlp, pl.lib, "dp_forces_mlp"));
+        CK(cudaLibraryGetKernel(&pl.energy_mlp, pl.lib, "dp_energy_mlp"));
+        CK(cudaLibraryGetKernel(&pl.virial_mlp, pl.lib, "dp_virial_mlp"));
+    }
     if (src.find("dp_batch_steps_128") != std::string::npos) {
         CK(cudaLibraryGetKernel(&pl.batch[0], pl.lib, "dp_batch_steps_128"));
         CK(cudaLibraryGetKernel(&pl.batch[1], pl.lib, "dp_batch_steps_256"));
@@ -859,6 +868,9 @@ struct dp_sim {
     double r_cut = 1.0;
     PairLib lib;
     bool lib_valid = false;
+
+    // pair surrogate (DP_PREC_MLP)
+    const dp_mlp_dev* mlp_dev = nullptr;
 
     // pair parameters
     int pmode = DP_PAIR_CONST;
@@ -1162,8 +1174,19 @@ static void fill_pair_args(const dp_sim* s, dp_pair_args& a, double* out) {
 static int launch_pair(dp_sim* s, cudaKernel_t k, double* out, long long* launches) {
     dp_pair_args a;
     fill_pair_args(s, a, out);
-    void* args[] = {&a};
-    CK(cudaLaunchKernel((const void*)k, dim3(grid_for(s->n, kBlock)), dim3(kBlock), args, 0, s->stream));
+    if (s->precision == DP_PREC_MLP) {
+        cudaKernel_t km = nullptr;
+        if (k == s->lib.forces) km = s->lib.forces_mlp;
+        else if (k == s->lib.energy) km = s->lib.energy_mlp;
+        else if (k == s->lib.virial) km = s->lib.virial_mlp;
+        if (!km) return fail(DP_ERR_ARG, "this quantity is not available with the pair surrogate");
+        const dp_mlp_dev* mp = s->mlp_dev;
+        void* args[] = {&a, &mp};
+        CK(cudaLaunchKernel((const void*)km, dim3(grid_for(s->n, kBlock)), dim3(kBlock), args, 0, s->stream));
+    } else {
+        void* args[] = {&a};
+        CK(cudaLaunchKernel((const void*)k, dim3(grid_for(s->n, kBlock)), dim3(kBlock), args, 0, s->stream));
+    }
     if (launches) *launches += 1;
     return DP_OK;
 }
@@ -1542,7 +1565,11 @@ static int rebuild_pair_lib(dp_sim* s);
 
 int dp_set_precision(dp_sim* s, int precision) {
     if (!s) return fail(DP_ERR_ARG, "null handle");
-    if (precision != DP_PREC_FP64 && precision != DP_PREC_FP32) return fail(DP_ERR_ARG, "unknown precision");
+    if (precision != DP_PREC_FP64 && precision != DP_PREC_FP32 && precision != DP_PREC_MLP)
+        return fail(DP_ERR_ARG, "unknown precision");
+    if (precision == DP_PREC_MLP && !s->mlp_dev) return fail(DP_ERR_ARG, "no pair surrogate attached (dp_set_mlp)");
+    if (precision == DP_PREC_MLP && s->pmode != DP_PAIR_CONST)
+        return fail(DP_ERR_ARG, "the pair surrogate needs constant sigma = epsilon = 1");
     if (precision == s->precision) return DP_OK;
     s->precision = precision;
     if (s->have_pot) RET(rebuild_pair_lib(s));
@@ -1697,7 +1724,8 @@ static std::string pair_program(int dim, int precision, int pmode, bool sig_one,
                                 const std::string& pot_src, bool with_batch) {
     std::string src;
     src += "#define DP_DIM " + std::to_string(dim) + "\n";
-    if (precision == DP_PREC_FP32) {
+    if (precision == DP_PREC_MLP) src += "#define DP_MLP 1\n";
+    if (precision == DP_PREC_FP32 || precision == DP_PREC_MLP) {
         src += "#define DP_REAL float\n#define DP_REAL_IS_FLOAT 1\n";
     } else {
         src += "#define DP_REAL double\n#define DP_REAL_IS_FLOAT 0\n";
@@ -1706,6 +1734,7 @@ static std::string pair_program(int dim, int precision, int pmode, bool sig_one,
     src += std::string("#define DP_SIGMA_ONE ") + (sig_one ? "1" : "0") + "\n";
     src += std::string("#define DP_EPS_ONE ") + (eps_one ? "1" : "0") + "\n";
     src += dp_src_common;
+    if (precision == DP_PREC_MLP) src += dp_src_mlp;
     src += "\n// ---- generated pair potential ----\n";
     src += pot_src;
     src += "\n// ---- pair kernels ----\n";
@@ -2546,6 +2575,209 @@ int dp_batch_last_forces(dp_batch* b, double* forces) {
     CK(cudaMemcpy(f.data(), b->force_out, f.size() * sizeof(float), cudaMemcpyDeviceToHost));
     for (long long i = 0; i < b->ntot; ++i)
         for (int k = 0; k < b->dim; ++k) forces[i * b->dim + k] = (double)f[(size_t)k * b->ntot + i];
+    return DP_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// pair surrogate network (training, evaluation)
+// ===========================================================================
+struct dp_mlp {
+    float *master = nullptr, *mo = nullptr, *ve = nullptr, *grad = nullptr, *norm = nullptr, *loss = nullptr;
+    dp_mlp_dev* dev = nullptr;
+    float* s = nullptr;
+    float2* t = nullptr;
+    long long n = 0;
+    long long* idx = nullptr;
+    long long idx_cap = 0;
+    float* losses = nullptr;
+    long long losses_cap = 0;
+    long long step = 0;
+    cudaStream_t stream = nullptr;
+};
+
+static int mlp_pack(dp_mlp* m) {
+    k_mlp_pack<<<4, 256, 0, m->stream>>>(m->master, m->norm, m->dev);
+    CK(cudaGetLastError());
+    return DP_OK;
+}
+
+static int mlp_grad_launch(dp_mlp* m, const float* s, const float2* t, const long long* idx, long long batch,
+                           float wf, bool accurate) {
+    MlpTrainArgs a;
+    a.s = s;
+    a.t = t;
+    a.idx = idx;
+    a.batch = batch;
+    a.mdev = m->dev;
+    a.master = m->master;
+    a.grad = m->grad;
+    a.loss = m->loss;
+    a.wf = wf;
+    a.inv_batch = 1.0f / (float)batch;
+    CK(cudaMemsetAsync(m->grad, 0, DP_MLP_NPARAM * sizeof(float), m->stream));
+    CK(cudaMemsetAsync(m->loss, 0, sizeof(float), m->stream));
+    const long long tiles = (batch + 15) / 16;
+    const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>((tiles + 7) / 8, 152LL * 4));
+    if (accurate)
+        k_mlp_grad<true><<<grid, 256, DP_MLP_GRAD_SMEM, m->stream>>>(a);
+    else
+        k_mlp_grad<false><<<grid, 256, DP_MLP_GRAD_SMEM, m->stream>>>(a);
+    CK(cudaGetLastError());
+    return DP_OK;
+}
+
+extern "C" {
+
+int dp_mlp_create(dp_mlp** out) {
+    if (!out) return fail(DP_ERR_ARG, "null argument");
+    *out = nullptr;
+    dp_mlp* m = new dp_mlp();
+    int rc = DP_OK;
+    if ((rc = dalloc_t(&m->master, DP_MLP_NPARAM)) || (rc = dalloc_t(&m->mo, DP_MLP_NPARAM)) ||
+        (rc = dalloc_t(&m->ve, DP_MLP_NPARAM)) || (rc = dalloc_t(&m->grad, DP_MLP_NPARAM)) ||
+        (rc = dalloc_t(&m->norm, 4)) || (rc = dalloc_t(&m->loss, 1)) || (rc = dalloc_t(&m->dev, 1))) {
+        dp_mlp_destroy(m);
+        return rc;
+    }
+    if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        dp_mlp_destroy(m);
+        return fail(DP_ERR_CUDA, "stream creation failed");
+    }
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_grad<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DP_MLP_GRAD_SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mlp_grad<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, DP_MLP_GRAD_SMEM);
+    if (e != cudaSuccess) {
+        dp_mlp_destroy(m);
+        return fail(DP_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+    }
+    *out = m;
+    return DP_OK;
+}
+
+int dp_mlp_destroy(dp_mlp* m) {
+    if (!m) return DP_OK;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    void* bufs[] = {m->master, m->mo, m->ve, m->grad, m->norm, m->loss, m->dev, m->s, m->t, m->idx, m->losses};
+    for (void* p : bufs)
+        if (p) cudaFree(p);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return DP_OK;
+}
+
+int dp_mlp_param_count(void) { return DP_MLP_NPARAM; }
+
+int dp_set_mlp(dp_sim* s, dp_mlp* m) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    if (!m && s->precision == DP_PREC_MLP) return fail(DP_ERR_ARG, "switch precision before detaching the surrogate");
+    s->mlp_dev = m ? m->dev : nullptr;
+    s->version++;
+    return DP_OK;
+}
+
+int dp_mlp_set_params(dp_mlp* m, const float* params, const float* norm) {
+    if (!m || !params || !norm) return fail(DP_ERR_ARG, "null argument");
+    CK(cudaMemcpyAsync(m->master, params, DP_MLP_NPARAM * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+    CK(cudaMemcpyAsync(m->norm, norm, 4 * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+    CK(cudaMemsetAsync(m->mo, 0, DP_MLP_NPARAM * sizeof(float), m->stream));
+    CK(cudaMemsetAsync(m->ve, 0, DP_MLP_NPARAM * sizeof(float), m->stream));
+    m->step = 0;
+    RET(mlp_pack(m));
+    CK(cudaStreamSynchronize(m->stream));
+    return DP_OK;
+}
+
+int dp_mlp_get_params(dp_mlp* m, float* params) {
+    if (!m || !params) return fail(DP_ERR_ARG, "null argument");
+    CK(cudaMemcpyAsync(params, m->master, DP_MLP_NPARAM * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    return DP_OK;
+}
+
+int dp_mlp_set_data(dp_mlp* m, const float* s, const float* targets, int64_t n) {
+    if (!m || !s || !targets || n < 1) return fail(DP_ERR_ARG, "bad training data");
+    RET(dalloc_t(&m->s, (size_t)n));
+    RET(dalloc_t(&m->t, (size_t)n));
+    CK(cudaMemcpy(m->s, s, (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(m->t, targets, (size_t)n * 2 * sizeof(float), cudaMemcpyHostToDevice));
+    m->n = n;
+    return DP_OK;
+}
+
+int dp_mlp_train(dp_mlp* m, int64_t steps, int batch, float lr0, float lr1, float wf, uint64_t seed, int accurate,
+                 float* losses) {
+    if (!m || !m->s) return fail(DP_ERR_ARG, "no training data");
+    if (steps < 1 || batch < 16) return fail(DP_ERR_ARG, "bad steps / batch");
+    if (batch > m->idx_cap) {
+        RET(dalloc_t(&m->idx, (size_t)batch));
+        m->idx_cap = batch;
+    }
+    if (steps > m->losses_cap) {
+        RET(dalloc_t(&m->losses, (size_t)steps));
+        m->losses_cap = steps;
+    }
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    for (long long k = 0; k < steps; ++k) {
+        // cosine decay from lr0 to lr1
+        const double frac = steps > 1 ? (double)k / (double)(steps - 1) : 1.0;
+        const float lr = (float)(lr1 + 0.5 * (lr0 - lr1) * (1.0 + std::cos(3.141592653589793 * frac)));
+        k_mlp_sample<<<grid_for(batch, kBlock), kBlock, 0, m->stream>>>(m->idx, batch, m->n, seed, m->step);
+        RET(mlp_grad_launch(m, m->s, m->t, m->idx, batch, wf, accurate != 0));
+        CK(cudaMemcpyAsync(m->losses + k, m->loss, sizeof(float), cudaMemcpyDeviceToDevice, m->stream));
+        ++m->step;
+        const float c1 = 1.0f / (1.0f - std::pow(b1, (float)m->step));
+        const float c2 = 1.0f / (1.0f - std::pow(b2, (float)m->step));
+        k_mlp_adam<<<grid_for(DP_MLP_NPARAM, kBlock), kBlock, 0, m->stream>>>(m->master, m->mo, m->ve, m->grad, lr,
+                                                                               b1, b2, eps, c1, c2);
+        RET(mlp_pack(m));
+    }
+    CK(cudaGetLastError());
+    if (losses) CK(cudaMemcpyAsync(losses, m->losses, (size_t)steps * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    return DP_OK;
+}
+
+int dp_mlp_eval(dp_mlp* m, const float* s, int64_t n, float* y, int accurate) {
+    if (!m || !s || !y || n < 1) return fail(DP_ERR_ARG, "bad arguments");
+    float* buf = nullptr;
+    RET(dalloc_t(&buf, (size_t)n * 3));
+    cudaError_t e = cudaMemcpyAsync(buf, s, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, m->stream);
+    const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>(((n + 15) / 16 + 7) / 8, 152LL * 8));
+    if (e == cudaSuccess) {
+        if (accurate)
+            k_mlp_eval<true><<<grid, 256, 0, m->stream>>>(buf, n, m->dev, buf + n);
+        else
+            k_mlp_eval<false><<<grid, 256, 0, m->stream>>>(buf, n, m->dev, buf + n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(y, buf + n, (size_t)n * 2 * sizeof(float), cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    cudaFree(buf);
+    if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("dp_mlp_eval: ") + cudaGetErrorString(e));
+    return DP_OK;
+}
+
+int dp_mlp_gradients(dp_mlp* m, const float* s, const float* targets, int64_t n, float wf, int accurate, float* grad,
+                     float* loss) {
+    if (!m || !s || !targets || !grad || n < 1) return fail(DP_ERR_ARG, "bad arguments");
+    float* buf = nullptr;
+    RET(dalloc_t(&buf, (size_t)n * 3));
+    cudaError_t e = cudaMemcpyAsync(buf, s, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, m->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(buf + n, targets, (size_t)n * 2 * sizeof(float), cudaMemcpyHostToDevice, m->stream);
+    int rc = DP_OK;
+    if (e == cudaSuccess) rc = mlp_grad_launch(m, buf, (const float2*)(buf + n), nullptr, n, wf, accurate != 0);
+    if (e == cudaSuccess && rc == DP_OK)
+        e = cudaMemcpyAsync(grad, m->grad, DP_MLP_NPARAM * sizeof(float), cudaMemcpyDeviceToHost, m->stream);
+    float l = 0.f;
+    if (e == cudaSuccess && rc == DP_OK) e = cudaMemcpyAsync(&l, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    cudaFree(buf);
+    if (rc != DP_OK) return rc;
+    if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("dp_mlp_gradients: ") + cudaGetErrorString(e));
+    if (loss) *loss = l / (float)n;
     return DP_OK;
 }
 

@@ -231,3 +231,104 @@ extern "C" __global__ void dp_eval_pair(const double* s_in, double* u, double* f
     f[i] = (double)dp_pair_f<real_t>(sr, sinv);
     c[i] = (double)dp_pair_c<real_t>(sr, sinv);
 }
+
+#if DP_MLP
+// ---------------------------------------------------------------------------
+// Pair surrogate path: the generated dp_pair_* functions hold the cheap
+// terms of the potential (in float32), the network of mlp_common.cuh the
+// costly ones. A warp owns 32 particles and walks their neighbour lists in
+// lock step: each round gathers one listed pair per particle, evaluates the
+// network on the 32 values of s = r^2 as two 16-row tensor-core tiles, sends
+// each row's result back to the lane owning the particle, and adds
+//   f/r = f_cheap(r)/r + (f/r)_nn,   u = u_cheap(r) + u_nn
+// for pairs inside r_cut (sigma = epsilon = 1 in this mode).
+template <int ACC>
+__device__ __forceinline__ void dp_mlp_pass(const dp_pair_args& a, const dp_mlp_dev* mg) {
+    constexpr int D = DP_DIM;
+    __shared__ dp_mlp_dev m;
+    __shared__ double red[32];
+    dp_mlp_load(&m, mg);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2;
+    const long long n = a.n;
+    const long long i = ((long long)blockIdx.x * (blockDim.x >> 5) + warp) * 32 + lane;
+    const bool active = i < n;
+    const shadow_t* __restrict__ sh = (const shadow_t*)a.shadow;
+    uint32_t ui[D];
+    if (active) dp_shadow_unpack<D>(sh[i], ui);
+    const int c = active ? a.cnt[i] : 0;
+    int maxc = c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) maxc = max(maxc, __shfl_xor_sync(0xffffffffu, maxc, o));
+    const float rc2 = (float)(a.rcut * a.rcut);
+    float f[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) f[k] = 0.0f;
+    double acc = 0.0;
+    for (int kk = 0; kk < maxc; ++kk) {
+        bool valid = false;
+        float q = m.x_mean, df[D];
+        if (kk < c) {
+            const int j = __ldg(a.nl + (long long)kk * n + i);
+            uint32_t uj[D];
+            dp_shadow_unpack<D>(__ldg(sh + j), uj);
+            const float qq = dp_shadow_q<D>(ui, uj, a.unit, df);
+            valid = qq <= rc2 && !(ACC == DP_ACC_VIRIAL && j <= i);
+            if (valid) q = qq;
+        }
+        float nn_u = 0.f, nn_f = 0.f;
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            const float sg = __shfl_sync(0xffffffffu, q, 16 * t + g);
+            const float sg8 = __shfl_sync(0xffffffffu, q, 16 * t + g + 8);
+            float y[2][2];
+            dp_mlp_tile<false>(m, sg, sg8, y);
+            const int o = lane - 16 * t;       // row of this lane's own pair in tile t
+            const int src = 4 * (o & 7);        // quad holding that row
+            const float r0u = __shfl_sync(0xffffffffu, y[0][0], src), r0f = __shfl_sync(0xffffffffu, y[0][1], src);
+            const float r1u = __shfl_sync(0xffffffffu, y[1][0], src), r1f = __shfl_sync(0xffffffffu, y[1][1], src);
+            if (o >= 0 && o < 16) {
+                nn_u = (o < 8) ? r0u : r1u;
+                nn_f = (o < 8) ? r0f : r1f;
+            }
+        }
+        if (valid) {
+            const float rinv = rsqrtf(q);
+            const float r = q * rinv;
+            const float fr = dp_pair_f<float>(r, rinv) * rinv + nn_f * m.f_scale;
+            if (ACC == DP_ACC_FORCE) {
+#pragma unroll
+                for (int k = 0; k < D; ++k) f[k] = fmaf(fr, df[k], f[k]);
+            } else if (ACC == DP_ACC_ENERGY) {
+                acc += (double)(dp_pair_u<float>(r, rinv) + nn_u * m.u_scale);
+            } else {
+                acc += (double)(fr * q);
+            }
+        }
+    }
+    if (ACC == DP_ACC_FORCE) {
+        if (active) {
+            bool finite = true;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                a.out[k * n + i] = (double)f[k];
+                finite = finite && isfinite(f[k]);
+            }
+            if (!finite) atomicExch(&a.status->nonfinite, 1);
+        }
+    } else {
+        const double v = dp_block_sum(acc, red);
+        if (threadIdx.x == 0) a.partial[blockIdx.x] = v;
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(256) dp_forces_mlp(dp_pair_args a, const dp_mlp_dev* mlp) {
+    dp_mlp_pass<DP_ACC_FORCE>(a, mlp);
+}
+extern "C" __global__ void __launch_bounds__(256) dp_energy_mlp(dp_pair_args a, const dp_mlp_dev* mlp) {
+    dp_mlp_pass<DP_ACC_ENERGY>(a, mlp);
+}
+extern "C" __global__ void __launch_bounds__(256) dp_virial_mlp(dp_pair_args a, const dp_mlp_dev* mlp) {
+    dp_mlp_pass<DP_ACC_VIRIAL>(a, mlp);
+}
+#endif

@@ -1,0 +1,168 @@
+"""Learned pair surrogate for costly SymPy potentials.
+
+A pair potential string is split into *cheap* terms (integer powers of r and
+constants: evaluated exactly by the generated code) and *costly* terms (anything
+with exp, cos, sin, log, non-integer powers, ...). A small network
+1 -> 64 -> 64 -> 2 in s = r^2 learns (u, f/r) of the costly terms; the GPU pair
+kernels then evaluate the cheap terms in float32 and the network on tensor
+cores (bf16 weights, fp32 accumulation). The network is trained on the GPU by
+the library's own forward/backward kernels (Adam) on samples of the
+code-generated float64 kernel, which stays the fallback and the judge
+(``PairSurrogate.errors``, force and NVE-drift comparisons in the tests and
+the benchmark).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import sympy as sp
+
+from . import _lib
+from . import codegen
+
+_COSTLY_FUNCS = (sp.exp, sp.log, sp.sin, sp.cos, sp.tan, sp.sinh, sp.cosh, sp.tanh, sp.erf, sp.erfc, sp.atan,
+                 sp.asin, sp.acos, sp.Abs, sp.Piecewise)
+
+
+def _is_costly(term: sp.Expr) -> bool:
+    if term.has(*_COSTLY_FUNCS):
+        return True
+    for p in term.atoms(sp.Pow):
+        if not p.exp.is_Integer:
+            return True
+    return False
+
+
+def split_costly(pair_potential_str: str) -> tuple[str, str]:
+    """(cheap, costly) SymPy strings whose sum is the potential."""
+    # distribute top-level products only: function arguments stay as written
+    expr = sp.expand(sp.sympify(pair_potential_str), deep=False, power_exp=False, power_base=False, log=False,
+                     multinomial=False)
+    cheap, costly = [], []
+    for term in sp.Add.make_args(expr):
+        (costly if _is_costly(term) else cheap).append(term)
+    return str(sp.Add(*cheap)), str(sp.Add(*costly))
+
+
+def _eval_codegen_fp64(pair_potential_str: str, r_cut: float, r: np.ndarray):
+    """u, f (= -du/dr) of a potential from the generated float64 device code."""
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    _lib.check(lib.dp_create(3, 1, _lib.DP_PREC_FP64, ctypes.byref(h)))
+    try:
+        box = np.array([10.0, 10.0, 10.0])
+        _lib.check(lib.dp_set_box(h, _lib.dptr(box)))
+        src, rc = codegen.make_pair_source(pair_potential_str, r_cut)
+        _lib.check(lib.dp_set_potential(h, src.encode(), rc))
+        rr = np.ascontiguousarray(r, dtype=np.float64)
+        u, f, c = np.empty_like(rr), np.empty_like(rr), np.empty_like(rr)
+        _lib.check(lib.dp_eval_potential(h, _lib.dptr(rr), rr.size, _lib.dptr(u), _lib.dptr(f), _lib.dptr(c)))
+        return u, f
+    finally:
+        lib.dp_destroy(h)
+
+
+class PairSurrogate:
+    """The trained network for the costly terms of one pair potential."""
+
+    def __init__(self, pair_potential_str: str, r_cut: float, r_min: float = 0.8, n_samples: int = 2 ** 20,
+                 seed: int = 0):
+        self.pair_potential_str = pair_potential_str
+        self.r_cut = float(r_cut)
+        self.r_min = float(r_min)
+        self.cheap_str, self.costly_str = split_costly(pair_potential_str)
+        if self.costly_str in ("0", ""):
+            raise ValueError("the potential has no costly terms to learn")
+        rng = np.random.default_rng(seed)
+        r = rng.uniform(self.r_min, self.r_cut, size=n_samples)
+        u, f = _eval_codegen_fp64(self.costly_str, self.r_cut, r)
+        s = r * r
+        fr = f / r
+        self.norm = np.array([s.mean(), 1.0 / s.std(), np.max(np.abs(u)), np.max(np.abs(fr))], dtype=np.float32)
+        targets = np.stack([u / self.norm[2], fr / self.norm[3]], axis=1).astype(np.float32)
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(lib.dp_mlp_create(ctypes.byref(h)))
+        self._h = h
+        self.nparam = int(lib.dp_mlp_param_count())
+        p = np.zeros(self.nparam, dtype=np.float32)
+        p[0:64] = rng.normal(0.0, 1.5, 64)
+        p[64:128] = rng.uniform(-2.0, 2.0, 64)
+        p[128:4224] = rng.normal(0.0, 1.0 / 8.0, 4096)
+        p[4288:4416] = rng.normal(0.0, 1.0 / 8.0, 128)
+        self.set_params(p)
+        _lib.check(lib.dp_mlp_set_data(h, _lib.fptr(np.ascontiguousarray(s, dtype=np.float32)),
+                                       _lib.fptr(np.ascontiguousarray(targets)), n_samples))
+        self.seed = seed
+        self.losses = np.zeros(0, dtype=np.float32)
+
+    # ------------------------------------------------------------- parameters
+    def set_params(self, params: np.ndarray) -> None:
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        _lib.check(_lib.load().dp_mlp_set_params(self._h, _lib.fptr(params), _lib.fptr(self.norm)))
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.nparam, dtype=np.float32)
+        _lib.check(_lib.load().dp_mlp_get_params(self._h, _lib.fptr(out)))
+        return out
+
+    # --------------------------------------------------------------- training
+    def train(self, steps: int = 6000, batch: int = 8192, lr0: float = 3e-3, lr1: float = 2e-5, wf: float = 1.0,
+              accurate: bool = False) -> np.ndarray:
+        """Adam on the GPU; returns the minibatch loss of every step."""
+        losses = np.empty(steps, dtype=np.float32)
+        _lib.check(_lib.load().dp_mlp_train(self._h, int(steps), int(batch), float(lr0), float(lr1), float(wf),
+                                            int(self.seed) & (2 ** 64 - 1), int(bool(accurate)),
+                                            _lib.fptr(losses)))
+        self.losses = np.concatenate([self.losses, losses])
+        return losses
+
+    def gradients(self, s: np.ndarray, targets: np.ndarray, wf: float = 1.0, accurate: bool = True):
+        s = np.ascontiguousarray(s, dtype=np.float32)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.empty(self.nparam, dtype=np.float32)
+        loss = ctypes.c_float(0.0)
+        _lib.check(_lib.load().dp_mlp_gradients(self._h, _lib.fptr(s), _lib.fptr(t), s.size, float(wf),
+                                                int(bool(accurate)), _lib.fptr(g), ctypes.byref(loss)))
+        return float(loss.value), g
+
+    # -------------------------------------------------------------- inference
+    def network(self, s: np.ndarray, accurate: bool = False) -> np.ndarray:
+        """Raw outputs y (n, 2) for inputs s = r^2."""
+        s = np.ascontiguousarray(np.asarray(s, dtype=np.float32).reshape(-1))
+        y = np.empty((s.size, 2), dtype=np.float32)
+        _lib.check(_lib.load().dp_mlp_eval(self._h, _lib.fptr(s), s.size, _lib.fptr(y), int(bool(accurate))))
+        return y
+
+    def costly_terms(self, r: np.ndarray):
+        """(u, f/r) of the costly terms predicted by the network."""
+        y = self.network(np.asarray(r, dtype=np.float64) ** 2).astype(np.float64)
+        return y[:, 0] * float(self.norm[2]), y[:, 1] * float(self.norm[3])
+
+    def errors(self, n: int = 200000, seed: int = 1) -> dict:
+        """Accuracy against the float64 generated code on fresh samples in
+        [r_min, r_cut]: RMS errors of u and f/r of the costly terms, relative to
+        the RMS of those terms, and relative to the total pair force f/r."""
+        rng = np.random.default_rng(seed)
+        r = rng.uniform(self.r_min, self.r_cut, size=n)
+        u_ref, f_ref = _eval_codegen_fp64(self.costly_str, self.r_cut, r)
+        fr_ref = f_ref / r
+        u_nn, fr_nn = self.costly_terms(r)
+        _, f_tot = _eval_codegen_fp64(self.pair_potential_str, self.r_cut, r)
+        rms = lambda v: float(np.sqrt(np.mean(v ** 2)))  # noqa: E731
+        return {"u_rel_rms": rms(u_nn - u_ref) / rms(u_ref), "fr_rel_rms": rms(fr_nn - fr_ref) / rms(fr_ref),
+                "fr_rel_rms_of_total": rms(fr_nn - fr_ref) / rms(f_tot / r),
+                "fr_max_abs": float(np.max(np.abs(fr_nn - fr_ref)))}
+
+    def cheap_source(self) -> tuple[str, float]:
+        return codegen.make_pair_source(self.cheap_str if self.cheap_str not in ("", "0") else "0*r", self.r_cut)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None:
+            try:
+                _lib.load().dp_mlp_destroy(h)
+            except Exception:
+                pass
+            self._h = None

@@ -74,7 +74,7 @@ class Simulation:
     _KNOWN_ENERGY_METHODS = {"neighbor list", "double loop", "double loop single core"}
     _KNOWN_FORCE_METHODS = {"neighbor list", "double loop", "double loop single core", "vectorized"}
     _KNOWN_CELL_LIST_METHODS = {"cell list", "double loop"}
-    _KNOWN_PRECISIONS = {"fp64": _lib.DP_PREC_FP64, "fp32": _lib.DP_PREC_FP32}
+    _KNOWN_PRECISIONS = {"fp64": _lib.DP_PREC_FP64, "fp32": _lib.DP_PREC_FP32, "mlp": _lib.DP_PREC_MLP}
 
     def __init__(self, particle_types=None, positions=None, box_vectors=None, image_positions=None,
                  velocities=None, betas=None, neighbor_list=None, positions_neighbour_list=None, masses=None,
@@ -117,6 +117,7 @@ class Simulation:
         d["_sigma_spec"] = 1.0
         d["_epsilon_spec"] = 1.0
         d["_pot_source"] = None
+        d["_surrogate"] = None
         d["_seed"] = int(np.random.randint(0, 2**62, dtype=np.int64))
         # dompap/Simulation.py:149-153
         self.set_pair_potential()
@@ -194,7 +195,8 @@ class Simulation:
             lib.dp_destroy(d["_h"])
             d["_h"] = None
         h = _lib.ctypes.c_void_p()
-        _lib.check(lib.dp_create(dim, n, d["_precision"], _lib.ctypes.byref(h)))
+        create_prec = _lib.DP_PREC_FP32 if d["_precision"] == _lib.DP_PREC_MLP else d["_precision"]
+        _lib.check(lib.dp_create(dim, n, create_prec, _lib.ctypes.byref(h)))
         d["_h"] = h
         d["_h_shape"] = (n, dim)
         d["_nl_count_base"] += rebuilds
@@ -252,8 +254,15 @@ class Simulation:
         dirty.clear()
         dirty.update(keep)
         if d.get("_pot_dirty"):
-            src = d["_pot_source"]
+            sur = d.get("_surrogate")
+            if d["_precision"] == _lib.DP_PREC_MLP and sur is not None:
+                src, _ = sur.cheap_source()
+                _lib.check(lib.dp_set_mlp(h, sur._h))
+            else:
+                src = d["_pot_source"]
             _lib.check(lib.dp_set_potential(h, src.encode(), float(self.pair_potential_r_cut)))
+            if d["_precision"] == _lib.DP_PREC_MLP:
+                _lib.check(lib.dp_set_precision(h, _lib.DP_PREC_MLP))
             d["_pot_dirty"] = False
             d["_nl_dirty"] = True
         if d.get("_params_dirty"):
@@ -400,7 +409,8 @@ class Simulation:
         for k, v in self.__dict__.items():
             if k in ("_h", "_h_shape"):
                 continue
-            nd[k] = deepcopy(v, memo) if k not in ("sigma_func", "epsilon_func", "_sigma_spec", "_epsilon_spec") else v
+            shared = ("sigma_func", "epsilon_func", "_sigma_spec", "_epsilon_spec", "_surrogate")
+            nd[k] = deepcopy(v, memo) if k not in shared else v
         nd["_h"] = None
         nd["_dev_newer"] = set()
         nd["_host_dirty"] = set()
@@ -670,11 +680,43 @@ class Simulation:
         self.__dict__["_int_dirty"] = True
 
     def set_precision(self, precision: str) -> None:
-        """'fp64' (parity) or 'fp32' (float32 pair forces, float64 integration and sums)."""
+        """'fp64' (parity), 'fp32' (float32 pair forces, float64 integration and
+        sums) or 'mlp' (the pair surrogate set with set_pair_surrogate)."""
         code = self._KNOWN_PRECISIONS[precision]
-        self.__dict__["_precision"] = code
+        d = self.__dict__
+        if code == _lib.DP_PREC_MLP and d.get("_surrogate") is None:
+            raise ValueError("set_pair_surrogate() first")
+        old = d["_precision"]
+        d["_precision"] = code
         if self._h is not None:
-            _lib.check(self._lib().dp_set_precision(self._h, code))
+            if old == _lib.DP_PREC_MLP or code == _lib.DP_PREC_MLP:
+                if old == _lib.DP_PREC_MLP:
+                    _lib.check(self._lib().dp_set_precision(self._h, _lib.DP_PREC_FP32))
+                d["_pot_dirty"] = True  # the cheap or the full potential source
+                if code != _lib.DP_PREC_MLP:
+                    _lib.check(self._lib().dp_set_precision(self._h, code))
+                self._push()
+            else:
+                _lib.check(self._lib().dp_set_precision(self._h, code))
+
+    def set_pair_surrogate(self, surrogate) -> None:
+        """Evaluate the costly terms of the current pair potential with a trained
+        ``dompap_gb300.mlp.PairSurrogate`` (precision 'mlp'); None returns to
+        float64 generated code."""
+        d = self.__dict__
+        if surrogate is None:
+            if d["_precision"] == _lib.DP_PREC_MLP:
+                self.set_precision("fp64")
+            d["_surrogate"] = None
+            return
+        if surrogate.pair_potential_str != self.pair_potential_str or surrogate.r_cut != float(
+                self.pair_potential_r_cut):
+            raise ValueError("the surrogate was trained for another pair potential or r_cut")
+        if not isinstance(d["_sigma_spec"], (float, int)) or float(d["_sigma_spec"]) != 1.0 or \
+                not isinstance(d["_epsilon_spec"], (float, int)) or float(d["_epsilon_spec"]) != 1.0:
+            raise ValueError("the pair surrogate needs sigma = epsilon = 1")
+        d["_surrogate"] = surrogate
+        self.set_precision("mlp")
 
     def number_of_particles(self) -> int:
         return self.__dict__["_positions"].shape[0]

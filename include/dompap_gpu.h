@@ -34,6 +34,7 @@ extern "C" {
 
 #define DP_PREC_FP64 0 /* float64 pair arithmetic (parity mode)                        */
 #define DP_PREC_FP32 1 /* float32 pair forces, float64 integration, wrap and sums      */
+#define DP_PREC_MLP 2  /* float32 cheap terms + tensor-core surrogate for costly terms */
 
 #define DP_NL_CELL 0   /* cell list + Verlet list (falls back to all pairs if < 3 cells) */
 #define DP_NL_ALLPAIRS 1 /* O(N^2) build, rows in ascending index order                */
@@ -223,6 +224,41 @@ int dp_batch_run(dp_batch *batch, int64_t steps, int sample_every, int nve, int 
 int dp_batch_observables(dp_batch *batch, double *out, int reset);
 /* (sum N, D) forces of the last recorded step (float32 values). */
 int dp_batch_last_forces(dp_batch *batch, double *forces);
+
+/* ---------------------------------------------------------------------------
+ * Pair surrogate: a 1 -> 64 -> 64 -> 2 tanh network of s = r^2 giving
+ * (u, f/r) of the costly terms of a pair potential, bf16 weights and fp32
+ * accumulation on tensor cores (mma.sync m16n8k16), trained by the library's
+ * own forward/backward kernels with Adam. No counterpart in dompap (it
+ * evaluates every term through its jitted SymPy lambdas,
+ * dompap/potential.py:43-66); the codegen path is its fallback and judge.
+ * Parameters (fp32, dp_mlp_param_count() of them): w1[64], b1[64],
+ * W2[64][64] (row = output unit), b2[64], W3[2][64], b3[2]; norm[4]:
+ * x_mean, 1/x_scale (x = (s - x_mean)/x_scale), u_scale, f_scale.
+ * ------------------------------------------------------------------------- */
+typedef struct dp_mlp dp_mlp;
+int dp_mlp_create(dp_mlp **out);
+int dp_mlp_destroy(dp_mlp *mlp);
+int dp_mlp_param_count(void);
+int dp_mlp_set_params(dp_mlp *mlp, const float *params, const float *norm);
+int dp_mlp_get_params(dp_mlp *mlp, float *params);
+/* Training set: n inputs s (float) and normalised targets (n, 2). */
+int dp_mlp_set_data(dp_mlp *mlp, const float *s, const float *targets, int64_t n);
+/* `steps` Adam steps on random minibatches of `batch` samples, learning rate
+ * decaying (cosine) from lr0 to lr1; loss (y0-t0)^2 + wf (y1-t1)^2. accurate
+ * selects the software tanh (else the hardware approximation, as inference
+ * uses). losses (may be NULL) receives the minibatch loss of every step. */
+int dp_mlp_train(dp_mlp *mlp, int64_t steps, int batch, float lr0, float lr1, float wf, uint64_t seed, int accurate,
+                 float *losses);
+/* Network outputs y (n, 2) for inputs s. */
+int dp_mlp_eval(dp_mlp *mlp, const float *s, int64_t n, float *y, int accurate);
+/* Gradient (dp_mlp_param_count() floats) and mean loss of a batch. */
+int dp_mlp_gradients(dp_mlp *mlp, const float *s, const float *targets, int64_t n, float wf, int accurate,
+                     float *grad, float *loss);
+/* Use `mlp` for the costly terms in the pair kernels of `sim` (the potential
+ * set with dp_set_potential is then the cheap remainder, with the full
+ * potential's shift). The network must outlive its use; NULL detaches. */
+int dp_set_mlp(dp_sim *sim, dp_mlp *mlp);
 
 #ifdef __cplusplus
 }
