@@ -2762,13 +2762,15 @@ int dp_mlp_eval(dp_mlp* m, const float* s, int64_t n, float* y, int accurate) {
 int dp_mlp_gradients(dp_mlp* m, const float* s, const float* targets, int64_t n, float wf, int accurate, float* grad,
                      float* loss) {
     if (!m || !s || !targets || !grad || n < 1) return fail(DP_ERR_ARG, "bad arguments");
+    // targets are read as float2: start them on an 8-byte boundary
+    const long long toff = (n + 1) & ~1LL;
     float* buf = nullptr;
-    RET(dalloc_t(&buf, (size_t)n * 3));
+    RET(dalloc_t(&buf, (size_t)(toff + 2 * n)));
     cudaError_t e = cudaMemcpyAsync(buf, s, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, m->stream);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(buf + n, targets, (size_t)n * 2 * sizeof(float), cudaMemcpyHostToDevice, m->stream);
+        e = cudaMemcpyAsync(buf + toff, targets, (size_t)n * 2 * sizeof(float), cudaMemcpyHostToDevice, m->stream);
     int rc = DP_OK;
-    if (e == cudaSuccess) rc = mlp_grad_launch(m, buf, (const float2*)(buf + n), nullptr, n, wf, accurate != 0);
+    if (e == cudaSuccess) rc = mlp_grad_launch(m, buf, (const float2*)(buf + toff), nullptr, n, wf, accurate != 0);
     if (e == cudaSuccess && rc == DP_OK)
         e = cudaMemcpyAsync(grad, m->grad, DP_MLP_NPARAM * sizeof(float), cudaMemcpyDeviceToHost, m->stream);
     float l = 0.f;
