@@ -49,6 +49,22 @@ WORKLOADS = {
     "lj500": (3, FCC, (5, 5, 5), 0.8442, "4*(r**-12-r**-6)", 2.5, 0.5, 1.0, 0.005, 0.1, 0.0),
 }
 
+EXPENSIVE_RAW = "4*(r**-12-r**-6) + 0.5*exp(-(r-1.5)**2/0.02) + 0.1*cos(4*r)*exp(-r)"
+# 4-point basis of the 4-D lattice used for the surrogate workload (16^4 cells x 4 = 262,144)
+BASIS_4D = ((0.0, 0.0, 0.0, 0.0), (0.5, 0.5, 0.0, 0.0), (0.0, 0.0, 0.5, 0.5), (0.5, 0.5, 0.5, 0.5))
+
+
+def expensive_string(r_cut=3.0):
+    """The costly test potential with its force shifted to zero at r_cut (the
+    smooth shift goes into the SymPy string; dompap only shifts the value)."""
+    import sympy as sp
+
+    r = sp.symbols("r")
+    u = sp.sympify(EXPENSIVE_RAW)
+    u_rc = float(sp.N(u.subs(r, r_cut), 30))
+    du_rc = float(sp.N(sp.diff(u, r).subs(r, r_cut), 30))
+    return f"{EXPENSIVE_RAW} - ({u_rc!r}) - (r - {float(r_cut)!r})*({du_rc!r})"
+
 
 def host_state(name, seed):
     """Lattice + jitter + Maxwell-Boltzmann velocities, as dompap builds it
@@ -376,11 +392,143 @@ def batched_variant(seed, steps=40, warmup=5, loop_sample=16):
                                  "how": "host loop of single-system runs (float32 forces, CUDA graphs per run)"}}
 
 
+def _lattice_sim(unit, cells, density, pot, r_cut, skin, temperature, dt, tau, seed, jitter, precision="fp64",
+                 kmax=256):
+    from dompap_gb300 import Simulation
+    from dompap_gb300.positions import generate_positions
+
+    dim = len(unit[0])
+    pos = generate_positions(unit, cells, (1.0,) * dim)
+    box = np.array(cells, dtype=np.float64)
+    scale = (pos.shape[0] / np.prod(box) / density) ** (1 / dim)
+    box, pos = box * scale, pos * scale
+    rng = np.random.default_rng(seed)
+    pos = pos + rng.normal(0.0, jitter, size=pos.shape)
+    img = np.floor(pos / box)
+    pos = pos - img * box
+    n = pos.shape[0]
+    np.random.seed(seed)
+    sim = Simulation(precision=precision)
+    sim.box_vectors = box
+    sim.positions = pos
+    sim.velocities = rng.normal(0.0, np.sqrt(temperature), size=pos.shape)
+    sim.betas = np.zeros_like(pos)
+    sim.image_positions = img.astype(np.int32)
+    sim.masses = np.ones((n, 1))
+    sim.particle_types = np.zeros((n, 1), dtype=np.int32)
+    sim.set_pair_potential(pot, r_cut)
+    sim.set_neighbor_list(skin=skin, max_number_of_neighbors=kmax, method_str="cell list")
+    sim.set_integrator(time_step=dt, target_temperature=temperature, temperature_damping_time=tau)
+    return sim
+
+
+def dimension_variant(name, seed, steps, warmup):
+    """The harmonic workload in 2-D (square 1024^2) or 4-D (hypercubic 32^4), FP64 and FP32 forces."""
+    out = {}
+    for prec in ("fp64", "fp32"):
+        sim = build_sim(name, seed, precision=prec)
+        n = sim.number_of_particles()
+        sim.run(warmup)
+        ms = sim.run_timed(steps)
+        out[prec] = {"value": n * steps / (ms / 1000.0), "unit": UNIT, "particles": n, "steps": steps,
+                     "ms_per_step": ms / steps}
+        if prec == "fp32":
+            f32 = sim.get_forces()
+            sim.set_precision("fp64")
+            f64 = sim.get_forces()
+            out[prec]["force_rel_rms_error_vs_fp64"] = float(
+                np.sqrt(np.mean((f32 - f64) ** 2) / max(np.mean(f64 ** 2), 1e-300)))
+        del sim
+    return out
+
+
+def wahnstrom_variant(seed, steps=300, warmup=20):
+    """Binary LJ 50:50 on a simple-cubic (80, 80, 40) lattice = 256,000 at density
+    0.75, sigma AA/AB/BB = 1.0/1.1/1.2, masses 2:1, r_cut = 2.5 sigma, T = 0.7,
+    dt = 0.004, damping 0.2, skin 0.5; per-type g(r) after the run."""
+    rng = np.random.default_rng(seed)
+    sim = _lattice_sim(((0.0, 0.0, 0.0),), (80, 80, 40), 0.75, "4*(r**-12-r**-6)", 2.5, 0.5, 0.7, 0.004, 0.2,
+                       seed, 0.02)
+    n = sim.number_of_particles()
+    types = np.zeros(n, dtype=np.int32)
+    types[rng.permutation(n)[: n // 2]] = 1
+    sim.set_types(types)
+    sim.set_masses(masses=np.where(types == 0, 2.0, 1.0))
+    sim.set_pair_potential_parameters(sigma=np.array([[1.0, 1.1], [1.1, 1.2]]), epsilon=np.array([[1.0, 1.0],
+                                                                                                   [1.0, 1.0]]))
+    sim.set_neighbor_list(skin=0.5, max_number_of_neighbors=256, method_str="cell list")
+    sim.run(warmup)
+    ms = sim.run_timed(steps)
+    value = n * steps / (ms / 1000.0)
+    bins = np.linspace(0.5, 3.5, 61)
+    g = {}
+    for a_t, b_t, key in ((0, 0, "AA"), (0, 1, "AB"), (1, 1, "BB")):
+        r, gr = sim.get_radial_distribution_function(bins, type_a=a_t, type_b=b_t)
+        g[key] = {"first_peak_r": float(r[np.argmax(gr)]), "first_peak_g": float(np.max(gr))}
+    return {"value": value, "unit": UNIT, "particles": n, "steps": steps, "ms_per_step": ms / steps,
+            "precision": "fp64 pair arithmetic, per-type sigma table", "T": sim.get_temperature(),
+            "U_per_particle": sim.get_potential_energy() / n, "g_r_first_peaks": g}
+
+
+def mlp_variant(seed, dim=3, steps=20, warmup=3):
+    """The costly potential (LJ + Gaussian + cos exp, force-shifted at r_cut = 3)
+    on fcc 64^3 = 1,048,576 (D=3) or 4-point 16^4 = 262,144 (D=4) at density
+    0.8: surrogate training, throughput of surrogate / FP32 / FP64 generated
+    code, and the surrogate's force error against FP64 on the same state."""
+    from dompap_gb300 import _lib
+    from dompap_gb300.mlp import PairSurrogate
+    from dompap_gb300.positions import FCC
+
+    pot = expensive_string(3.0)
+    t0 = time.perf_counter()
+    sur = PairSurrogate(pot, 3.0, r_min=0.8, n_samples=2 ** 20, seed=seed)
+    losses = sur.train()
+    t_train = time.perf_counter() - t0
+    acc = sur.errors()
+    unit, cells = (FCC, (64, 64, 64)) if dim == 3 else (BASIS_4D, (16, 16, 16, 16))
+    sim = _lattice_sim(unit, cells, 0.8, pot, 3.0, 0.3, 1.0, 0.004, 0.1, seed, 0.05,
+                       kmax=256 if dim == 3 else 512)
+    n = sim.number_of_particles()
+    lib = _lib.load()
+    res = {"particles": n, "dim": dim, "training_seconds": t_train, "training_steps": int(losses.size),
+           "final_minibatch_loss": float(losses[-1]), "surrogate_vs_fp64_codegen_on_samples": acc}
+    f64 = sim.get_forces()
+    ms = _lib.ctypes.c_float(0.0)
+    _lib.check(lib.dp_time_kernel(sim._h, _lib.DP_KERNEL_FORCES, 2, _lib.ctypes.byref(ms)))
+    res["fp64_codegen"] = {"force_kernel_ms": float(ms.value), "value_forces_only": n / (ms.value / 1000.0)}
+    sim.set_precision("fp32")
+    sim.run(warmup)
+    tms = sim.run_timed(steps)
+    f32 = sim.get_forces()
+    res["fp32_codegen"] = {"value": n * steps / (tms / 1000.0), "ms_per_step": tms / steps}
+    sim.set_precision("fp64")
+    f64 = sim.get_forces()
+    sim.set_pair_surrogate(sur)
+    fnn = sim.get_forces()
+    _lib.check(lib.dp_time_kernel(sim._h, _lib.DP_KERNEL_FORCES, 5, _lib.ctypes.byref(ms)))
+    res["surrogate"] = {"force_kernel_ms": float(ms.value),
+                        "force_rel_rms_error_vs_fp64": float(np.sqrt(np.mean((fnn - f64) ** 2) / np.mean(f64 ** 2)))}
+    sim.run(warmup)
+    tms = sim.run_timed(steps)
+    res["surrogate"].update({"value": n * steps / (tms / 1000.0), "ms_per_step": tms / steps})
+    res["fp32_codegen"]["force_rel_rms_error_vs_fp64"] = float(
+        np.sqrt(np.mean((f32 - f64) ** 2) / np.mean(f64 ** 2)))
+    res["value"] = res["surrogate"]["value"]
+    res["unit"] = UNIT
+    del sim
+    return res
+
+
 def variants(args, main_sim):
     out = {}
     for name, fn in (("fp32_force", lambda: fp32_variant(args.workload, args.seed + 7, min(args.steps, 1000),
                                                          args.warmup)),
-                     ("batched_4096_lj", lambda: batched_variant(args.seed + 11))):
+                     ("batched_4096_lj", lambda: batched_variant(args.seed + 11)),
+                     ("harmonic2d", lambda: dimension_variant("harmonic2d", args.seed + 3, 500, 10)),
+                     ("harmonic4d", lambda: dimension_variant("harmonic4d", args.seed + 4, 300, 10)),
+                     ("wahnstrom_256000", lambda: wahnstrom_variant(args.seed + 5)),
+                     ("mlp_surrogate_3d", lambda: mlp_variant(args.seed + 6, dim=3)),
+                     ("mlp_surrogate_4d", lambda: mlp_variant(args.seed + 8, dim=4))):
         try:
             out[name] = fn()
         except Exception as exc:  # reported, not hidden

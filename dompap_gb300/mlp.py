@@ -108,7 +108,7 @@ class PairSurrogate:
         return out
 
     # --------------------------------------------------------------- training
-    def train(self, steps: int = 6000, batch: int = 8192, lr0: float = 3e-3, lr1: float = 2e-5, wf: float = 1.0,
+    def train(self, steps: int = 30000, batch: int = 16384, lr0: float = 2e-3, lr1: float = 1e-6, wf: float = 1.0,
               accurate: bool = False) -> np.ndarray:
         """Adam on the GPU; returns the minibatch loss of every step."""
         losses = np.empty(steps, dtype=np.float32)

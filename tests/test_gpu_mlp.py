@@ -27,7 +27,7 @@ def surrogate():
     from dompap_gb300.mlp import PairSurrogate
 
     sur = PairSurrogate(expensive_string(), 3.0, r_min=0.8, n_samples=2 ** 20, seed=0)
-    sur.train(steps=6000, batch=8192)
+    sur.train(steps=30000, batch=16384, lr0=2e-3, lr1=1e-6)
     return sur
 
 
@@ -63,8 +63,8 @@ def test_training_reaches_accuracy(surrogate):
     err = surrogate.errors()
     print("surrogate accuracy vs float64 codegen:", err, "final loss", float(surrogate.losses[-1]))
     assert surrogate.losses[-1] < surrogate.losses[0] * 1e-3
-    assert err["fr_rel_rms"] < 2e-2
-    assert err["fr_rel_rms_of_total"] < 1e-3
+    assert err["fr_rel_rms"] < 1e-2
+    assert err["fr_rel_rms_of_total"] < 1e-4
 
 
 def _liquid(seed=0, cells=(10, 10, 10)):
@@ -99,7 +99,7 @@ def test_surrogate_forces_and_energy(surrogate):
           f"W/N {wnn / n:.5f} vs {w64 / n:.5f}")
     assert err < 1e-3
     assert abs(unn - u64) / n < 2e-3
-    assert abs(wnn - w64) / n < 1e-2
+    assert abs(wnn - w64) / n < 2e-2
     sim.set_pair_surrogate(None)
     assert np.array_equal(sim.get_forces(), f64)
 
