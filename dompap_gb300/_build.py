@@ -41,7 +41,8 @@ def write_embedded() -> str:
     os.makedirs(BUILD, exist_ok=True)
     parts = []
     for name, sym in (("dp_common.cuh", "dp_src_common"), ("pair_kernels.cuh", "dp_src_pair"),
-                      ("batch_kernels.cuh", "dp_src_batch"), ("mlp_common.cuh", "dp_src_mlp")):
+                      ("batch_kernels.cuh", "dp_src_batch"), ("mlp_common.cuh", "dp_src_mlp"),
+                      ("dp_ff.cuh", "dp_src_ff")):
         with open(os.path.join(CSRC, name)) as fh:
             text = fh.read()
         if ')DPSRC"' in text:
@@ -99,13 +100,16 @@ def check_pair_kernels(verbose: bool = True) -> None:
         pair = fh.read()
     with open(os.path.join(CSRC, "batch_kernels.cuh")) as fh:
         batch = fh.read()
+    with open(os.path.join(CSRC, "dp_ff.cuh")) as fh:
+        ffsrc = fh.read()
     for dim in (2, 3, 4):
         for real, is_float in (("double", 0), ("float", 1)):
             for pmode in (0, 1, 2):
                 src = (f"#define DP_DIM {dim}\n#define DP_REAL {real}\n#define DP_REAL_IS_FLOAT {is_float}\n"
                        f"#define DP_PMODE {pmode}\n#define DP_SIGMA_ONE {int(pmode == 0)}\n"
-                       f"#define DP_EPS_ONE {int(pmode == 0)}\n#include <cstdint>\n"
-                       + common + SAMPLE_POTENTIAL + pair + (batch if is_float and pmode == 0 else ""))
+                       f"#define DP_EPS_ONE {int(pmode == 0)}\n#define DP_FF {1 - is_float}\n#include <cstdint>\n"
+                       + common + (ffsrc if not is_float else "") + SAMPLE_POTENTIAL + pair
+                       + (batch if is_float and pmode == 0 else ""))
                 path = os.path.join(BUILD, f"pair_check_{dim}_{real}_{pmode}.cu")
                 with open(path, "w") as fh:
                     fh.write(src)

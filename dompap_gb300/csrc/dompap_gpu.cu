@@ -105,11 +105,19 @@ __global__ void k_soa_to_aos_i32(const int32_t* __restrict__ in, int32_t* __rest
 struct ShadowArgs {
     const double* pos;
     void* shadow;
+    void* pos64;
     dp_dev_status* st;
     long long n;
     double scale[DP_MAX_DIM];
+    double scale64[DP_MAX_DIM];
     double box[DP_MAX_DIM];
 };
+
+// 64-bit fixed point of one coordinate, wrapped into [0, L) first when needed.
+__device__ __forceinline__ unsigned long long fixed64_wrapped(double x, double L, double scale64) {
+    if (!(x >= 0.0 && x < L)) x -= floor(x / L) * L;
+    return dp_fixed64_of(x * scale64);
+}
 
 // Fixed-point shadow of all positions; flags coordinates outside
 // [-L/4, 5L/4), for which the single-shift image is not the nearest one.
@@ -118,14 +126,17 @@ __global__ void k_shadow(ShadowArgs a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     uint32_t u[D];
+    unsigned long long X[D];
     bool far = false;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         const double x = a.pos[k * a.n + i];
         u[k] = dp_fixed(x, a.scale[k]);
+        X[k] = fixed64_wrapped(x, a.box[k], a.scale64[k]);
         far = far || !(x >= -0.25 * a.box[k] && x < 1.25 * a.box[k]);
     }
     ((typename dp_shadow_t<D>::type*)a.shadow)[i] = dp_shadow_pack<D>(u);
+    ((typename dp_fixed64_t<D>::type*)a.pos64)[i] = dp_fixed64_pack<D>(X);
     if (far) atomicExch(&a.st->far, 1);
 }
 
@@ -451,6 +462,7 @@ struct IntArgs {
     const double* force;
     int32_t* img;
     void* shadow;
+    void* pos64;
     const double* pos_ref;
     const void* shadow_ref;
     const uint8_t* mclass;
@@ -460,6 +472,7 @@ struct IntArgs {
     long long n;
     double box[DP_MAX_DIM];
     double scale[DP_MAX_DIM];
+    double scale64[DP_MAX_DIM];
     float unit[DP_MAX_DIM];
     double thr;  // (skin/2)^2
     float thr_lo, thr_hi;
@@ -518,7 +531,7 @@ __device__ __forceinline__ double wrap_axis(double x, double L, int32_t& image) 
 // position is converted to fixed point once; a value outside [0, 2^32) is the
 // only case that needs the wrap (done exactly as wrap_into_box), and the skin
 // test reads the shadows (float64 only near the threshold).
-template <int D, int MASSMODE, bool NVE>
+template <int D, int MASSMODE, bool NVE, bool WRITE64>
 __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st->far = 0;  // every position is wrapped below
@@ -530,6 +543,7 @@ __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
         float z[4];
         if (!NVE) dp_normals4(a.seed, (unsigned long long)(a.st->step + a.step_offset), (uint32_t)i, z);
         uint32_t u[D];
+        unsigned long long X[D];
         double xs[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
@@ -545,21 +559,38 @@ __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
                 a.beta[o] = bn;
             }
             x = x + v * a.dt;
-            const long long t = __double2ll_rd(x * a.scale[k]);
-            if (t < 0 || t >= 4294967296LL) {
-                int32_t im = a.img[o];
-                x = wrap_axis(x, a.box[k], im);
-                a.img[o] = im;
-                u[k] = dp_fixed(x, a.scale[k]);
-                bad = bad || !isfinite(x);
+            if (WRITE64) {
+                // one product gives the wrap test (its bit pattern, an integer
+                // compare), the 64-bit fixed point and the 32-bit shadow
+                double p = x * a.scale64[k];
+                const long long pb = __double_as_longlong(p);
+                if (!(pb >= 0 && pb < 0x43F0000000000000LL)) {  // p outside [0, 2^64)
+                    int32_t im = a.img[o];
+                    x = wrap_axis(x, a.box[k], im);
+                    a.img[o] = im;
+                    bad = bad || !isfinite(x);
+                    p = (x >= 0.0 && x < a.box[k]) ? x * a.scale64[k] : 0.0;
+                }
+                X[k] = dp_fixed64_of(p);
+                u[k] = (uint32_t)(X[k] >> 32);
             } else {
-                u[k] = (uint32_t)t;
+                const long long t = __double2ll_rd(x * a.scale[k]);
+                if (t < 0 || t >= 4294967296LL) {
+                    int32_t im = a.img[o];
+                    x = wrap_axis(x, a.box[k], im);
+                    a.img[o] = im;
+                    u[k] = dp_fixed(x, a.scale[k]);
+                    bad = bad || !isfinite(x);
+                } else {
+                    u[k] = (uint32_t)t;
+                }
             }
             a.vel[o] = v;
             a.pos[o] = x;
             xs[k] = x;
         }
         ((typename dp_shadow_t<D>::type*)a.shadow)[i] = dp_shadow_pack<D>(u);
+        if (WRITE64) ((typename dp_fixed64_t<D>::type*)a.pos64)[i] = dp_fixed64_pack<D>(X);
         SkinArgs sa;
         sa.pos_ref = a.pos_ref;
         sa.shadow_ref = a.shadow_ref;
@@ -631,6 +662,7 @@ __global__ void k_wrap(IntArgs a) {
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st->far = 0;
     if (i >= a.n) return;
     uint32_t u[D];
+    unsigned long long X[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         const long long o = k * a.n + i;
@@ -640,8 +672,10 @@ __global__ void k_wrap(IntArgs a) {
         a.pos[o] = x;
         if (im != im0) a.img[o] = im;
         u[k] = dp_fixed(x, a.scale[k]);
+        X[k] = fixed64_wrapped(x, a.box[k], a.scale64[k]);
     }
     ((typename dp_shadow_t<D>::type*)a.shadow)[i] = dp_shadow_pack<D>(u);
+    ((typename dp_fixed64_t<D>::type*)a.pos64)[i] = dp_fixed64_pack<D>(X);
 }
 
 // Pair-distance histogram for g(r) (dompap/positions.py:58-87): all ordered
@@ -844,6 +878,7 @@ struct dp_sim {
     int32_t* img = nullptr;
     void* shadow = nullptr;
     void* shadow_ref = nullptr;
+    void* pos64 = nullptr;
     size_t shadow_bytes = 0;
     double *bk_pos = nullptr, *bk_vel = nullptr, *bk_beta = nullptr;
     int32_t* bk_img = nullptr;
@@ -877,6 +912,7 @@ struct dp_sim {
     int ntypes = 1;
     double sigma = 1.0, epsilon = 1.0, sig_max = 1.0;
     double *sig_tab = nullptr, *eps_tab = nullptr, *isig_tab = nullptr;
+    float2* ff_tab = nullptr;  // (sigma, 1/sigma, epsilon) double-float triples per type pair
 
     // neighbour list
     double skin = 1.0;
@@ -973,9 +1009,11 @@ static int launch_shadow(dp_sim* s) {
     ShadowArgs a{};
     a.pos = s->pos;
     a.shadow = s->shadow;
+    a.pos64 = s->pos64;
     a.st = s->dstat;
     a.n = s->n;
     fill_scale(s, a.scale, nullptr);
+    for (int k = 0; k < DP_MAX_DIM; ++k) a.scale64[k] = 18446744073709551616.0 / ((k < s->dim) ? s->box[k] : 1.0);
     for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
     CK(cudaMemsetAsync(&s->dstat->far, 0, sizeof(int32_t), s->stream));
     const unsigned g = grid_for(s->n, kBlock);
@@ -1146,6 +1184,8 @@ static void fill_pair_args(const dp_sim* s, dp_pair_args& a, double* out) {
     a.sig_tab = s->sig_tab;
     a.eps_tab = s->eps_tab;
     a.isig_tab = s->isig_tab;
+    a.ff_tab = s->ff_tab;
+    a.pos64 = s->pos64;
     a.out = out;
     a.partial = s->partial;
     a.status = s->dstat;
@@ -1153,6 +1193,11 @@ static void fill_pair_args(const dp_sim* s, dp_pair_args& a, double* out) {
     a.ntypes = s->ntypes;
     for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
     fill_scale(s, nullptr, a.unit);
+    for (int k = 0; k < DP_MAX_DIM; ++k) {
+        const double u64 = ((k < s->dim) ? s->box[k] : 1.0) / 18446744073709551616.0;
+        a.unit64_hi[k] = (float)u64;
+        a.unit64_lo[k] = (float)(u64 - (double)(float)u64);
+    }
     a.sigma = s->sigma;
     a.inv_sigma = 1.0 / s->sigma;
     a.epsilon = s->epsilon;
@@ -1199,6 +1244,7 @@ static void fill_int_args(const dp_sim* s, IntArgs& a, long long step_offset) {
     a.force = s->force;
     a.img = s->img;
     a.shadow = s->shadow;
+    a.pos64 = s->pos64;
     a.pos_ref = s->pos_ref;
     a.shadow_ref = s->shadow_ref;
     a.mclass = s->mclass;
@@ -1208,6 +1254,7 @@ static void fill_int_args(const dp_sim* s, IntArgs& a, long long step_offset) {
     a.n = s->n;
     for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
     fill_scale(s, a.scale, a.unit);
+    for (int k = 0; k < DP_MAX_DIM; ++k) a.scale64[k] = 18446744073709551616.0 / ((k < s->dim) ? s->box[k] : 1.0);
     a.thr = (0.5 * s->skin) * (0.5 * s->skin);
     bracket(s, 0.5 * s->skin, &a.thr_lo, &a.thr_hi);
     a.dt = s->dt;
@@ -1231,14 +1278,23 @@ static void fill_int_args(const dp_sim* s, IntArgs& a, long long step_offset) {
     a.step_offset = step_offset;
 }
 
-template <int D, bool NVE>
-static void launch_integrate_d(dp_sim* s, const IntArgs& a) {
+template <int D, bool NVE, bool W64>
+static void launch_integrate_dw(dp_sim* s, const IntArgs& a) {
     const unsigned g = grid_for(s->n, kBlock);
     switch (s->mass_mode) {
-        case 0: k_integrate<D, 0, NVE><<<g, kBlock, 0, s->stream>>>(a); break;
-        case 1: k_integrate<D, 1, NVE><<<g, kBlock, 0, s->stream>>>(a); break;
-        default: k_integrate<D, 2, NVE><<<g, kBlock, 0, s->stream>>>(a); break;
+        case 0: k_integrate<D, 0, NVE, W64><<<g, kBlock, 0, s->stream>>>(a); break;
+        case 1: k_integrate<D, 1, NVE, W64><<<g, kBlock, 0, s->stream>>>(a); break;
+        default: k_integrate<D, 2, NVE, W64><<<g, kBlock, 0, s->stream>>>(a); break;
     }
+}
+
+// The 64-bit fixed point is only read by the float64-parity pair kernels.
+template <int D, bool NVE>
+static void launch_integrate_d(dp_sim* s, const IntArgs& a) {
+    if (s->precision == DP_PREC_FP64)
+        launch_integrate_dw<D, NVE, true>(s, a);
+    else
+        launch_integrate_dw<D, NVE, false>(s, a);
 }
 
 static int launch_integrate(dp_sim* s, int kind, long long step_offset, long long* launches) {
@@ -1513,7 +1569,9 @@ int dp_create(int dim, int64_t n, int precision, dp_sim** out) {
         (rc = dalloc_t(&s->bk_img, nd)) || (rc = dalloc_t(&s->cnt, (size_t)n)))
         return cleanup();
     s->shadow_bytes = (size_t)n * (dim == 2 ? 8 : 16);
-    if ((rc = dalloc(&s->shadow, s->shadow_bytes)) || (rc = dalloc(&s->shadow_ref, s->shadow_bytes))) return cleanup();
+    if ((rc = dalloc(&s->shadow, s->shadow_bytes)) || (rc = dalloc(&s->shadow_ref, s->shadow_bytes)) ||
+        (rc = dalloc(&s->pos64, (size_t)n * (dim == 2 ? 16 : 32))))
+        return cleanup();
     if (cudaMemset(s->shadow, 0, s->shadow_bytes) != cudaSuccess ||
         cudaMemset(s->shadow_ref, 0, s->shadow_bytes) != cudaSuccess) {
         rc = fail(DP_ERR_CUDA, "cudaMemset failed");
@@ -1546,7 +1604,8 @@ int dp_destroy(dp_sim* s) {
     if (!s) return DP_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_graphs(s);
-    void* bufs[] = {s->pos, s->vel, s->beta, s->force, s->pos_ref, s->img, s->shadow, s->shadow_ref, s->bk_pos,
+    void* bufs[] = {s->pos, s->vel, s->beta, s->force, s->pos_ref, s->img, s->shadow, s->shadow_ref, s->pos64,
+                    s->ff_tab, s->bk_pos,
                     s->bk_vel, s->bk_beta, s->bk_img, s->mclass, s->mcoef, s->class_mass_dev, s->mass, s->types,
                     s->sig_tab, s->eps_tab, s->isig_tab, s->nl, s->cnt, s->cell_cnt, s->cell_mem, s->dstat,
                     s->partial, s->dsum};
@@ -1570,6 +1629,7 @@ int dp_set_precision(dp_sim* s, int precision) {
     if (precision == DP_PREC_MLP && !s->mlp_dev) return fail(DP_ERR_ARG, "no pair surrogate attached (dp_set_mlp)");
     if (precision == DP_PREC_MLP && s->pmode != DP_PAIR_CONST)
         return fail(DP_ERR_ARG, "the pair surrogate needs constant sigma = epsilon = 1");
+    if (precision == DP_PREC_FP64 && s->have_box) RET(launch_shadow(s));  // refresh the 64-bit fixed point
     if (precision == s->precision) return DP_OK;
     s->precision = precision;
     if (s->have_pot) RET(rebuild_pair_lib(s));
@@ -1725,6 +1785,7 @@ static std::string pair_program(int dim, int precision, int pmode, bool sig_one,
     std::string src;
     src += "#define DP_DIM " + std::to_string(dim) + "\n";
     if (precision == DP_PREC_MLP) src += "#define DP_MLP 1\n";
+    if (precision == DP_PREC_FP64) src += "#define DP_FF 1\n";
     if (precision == DP_PREC_FP32 || precision == DP_PREC_MLP) {
         src += "#define DP_REAL float\n#define DP_REAL_IS_FLOAT 1\n";
     } else {
@@ -1735,6 +1796,7 @@ static std::string pair_program(int dim, int precision, int pmode, bool sig_one,
     src += std::string("#define DP_EPS_ONE ") + (eps_one ? "1" : "0") + "\n";
     src += dp_src_common;
     if (precision == DP_PREC_MLP) src += dp_src_mlp;
+    if (precision == DP_PREC_FP64) src += dp_src_ff;
     src += "\n// ---- generated pair potential ----\n";
     src += pot_src;
     src += "\n// ---- pair kernels ----\n";
@@ -1792,6 +1854,15 @@ int dp_set_pair_params(dp_sim* s, int mode, int ntypes, const double* sigma, con
         CK(cudaMemcpy(s->sig_tab, sigma, m * sizeof(double), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(s->eps_tab, epsilon, m * sizeof(double), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(s->isig_tab, inv.data(), m * sizeof(double), cudaMemcpyHostToDevice));
+        std::vector<float2> ff(3 * m);
+        auto split = [](double v) { return make_float2((float)v, (float)(v - (double)(float)v)); };
+        for (size_t t = 0; t < m; ++t) {
+            ff[3 * t + 0] = split(sigma[t]);
+            ff[3 * t + 1] = split(inv[t]);
+            ff[3 * t + 2] = split(epsilon[t]);
+        }
+        RET(dalloc_t(&s->ff_tab, ff.size()));
+        CK(cudaMemcpy(s->ff_tab, ff.data(), ff.size() * sizeof(float2), cudaMemcpyHostToDevice));
         s->ntypes = ntypes;
     } else if (mode == DP_PAIR_DENSE) {
         const size_t m = (size_t)s->n * s->n;

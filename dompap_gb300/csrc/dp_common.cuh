@@ -39,6 +39,8 @@ struct dp_pair_args {
     const double* sig_tab;
     const double* eps_tab;
     const double* isig_tab;  // 1 / sigma per type pair (DP_PMODE == 1)
+    const float2* ff_tab;    // DP_PMODE == 1: (sigma, 1/sigma, epsilon) as double-float triples
+    const void* pos64;       // 64-bit fixed-point positions (X = x 2^64 / L), one vector per particle
     double* out;
     double* partial;
     dp_dev_status* status;
@@ -47,6 +49,8 @@ struct dp_pair_args {
     int pad0;
     double box[DP_MAX_DIM];
     float unit[DP_MAX_DIM];  // L / 2^32 per axis
+    float unit64_hi[DP_MAX_DIM];  // L / 2^64 per axis as a double-float
+    float unit64_lo[DP_MAX_DIM];
     double sigma;            // DP_PMODE == 0
     double inv_sigma;        // DP_PMODE == 0
     double epsilon;          // DP_PMODE == 0
@@ -118,6 +122,57 @@ __device__ __forceinline__ uint32_t dp_fixed(double x, double scale /* 2^32 / L 
     const long long t = __double2ll_rd(x * scale);
     return (uint32_t)(unsigned long long)t;
 }
+
+// 64-bit fixed point X = floor(x 2^64 / L) for 0 <= x < L (exact product
+// rounding aside), the source of the exact nearest-image displacement
+// (int64)(X_i - X_j) of the double-float pair arithmetic.
+template <int D>
+struct dp_fixed64_t {
+    typedef ulonglong4 type;
+};
+template <>
+struct dp_fixed64_t<2> {
+    typedef ulonglong2 type;
+};
+template <int D>
+__device__ __forceinline__ void dp_fixed64_unpack(const typename dp_fixed64_t<D>::type& v, unsigned long long* X);
+template <>
+__device__ __forceinline__ void dp_fixed64_unpack<2>(const ulonglong2& v, unsigned long long* X) {
+    X[0] = v.x;
+    X[1] = v.y;
+}
+template <>
+__device__ __forceinline__ void dp_fixed64_unpack<3>(const ulonglong4& v, unsigned long long* X) {
+    X[0] = v.x;
+    X[1] = v.y;
+    X[2] = v.z;
+}
+template <>
+__device__ __forceinline__ void dp_fixed64_unpack<4>(const ulonglong4& v, unsigned long long* X) {
+    X[0] = v.x;
+    X[1] = v.y;
+    X[2] = v.z;
+    X[3] = v.w;
+}
+template <int D>
+__device__ __forceinline__ typename dp_fixed64_t<D>::type dp_fixed64_pack(const unsigned long long* X);
+template <>
+__device__ __forceinline__ ulonglong2 dp_fixed64_pack<2>(const unsigned long long* X) {
+    return make_ulonglong2(X[0], X[1]);
+}
+template <>
+__device__ __forceinline__ ulonglong4 dp_fixed64_pack<3>(const unsigned long long* X) {
+    return make_ulonglong4(X[0], X[1], X[2], 0ull);
+}
+template <>
+__device__ __forceinline__ ulonglong4 dp_fixed64_pack<4>(const unsigned long long* X) {
+    return make_ulonglong4(X[0], X[1], X[2], X[3]);
+}
+
+// Both fixed-point forms of one coordinate from the float64 product
+// p = x 2^64 / L: the 64-bit one and its upper 32 bits (the shadow). The
+// coordinate must lie in [0, L); a product rounded up to 2^64 saturates.
+__device__ __forceinline__ unsigned long long dp_fixed64_of(double p) { return __double2ull_rd(p); }
 
 template <int D>
 struct dp_shadow_t;

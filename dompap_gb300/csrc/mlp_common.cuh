@@ -5,7 +5,7 @@
 //   h1 = tanh(w1 * x + b1)                 64 units (bf16 weights)
 //   h2 = tanh(W2 h1 + b2)                  64 x 64 bf16 weights, fp32 accumulate (mma)
 //   y  = W3 h2 + b3                        2 outputs (bf16 weights)
-//   u_nn = y0 * u_scale,  (f/r)_nn = y1 * f_scale
+//   u_nn = y0 * u_scale,  (f r)_nn = y1 * f_scale,  (f/r)_nn = (f r)_nn / s
 // A warp evaluates 16 pairs per call ("tile"): the 16 x 64 layer-1
 // activations are produced directly in the A-fragment layout of
 // mma.sync.m16n8k16 (row = pair, column = unit), split into a bf16 high part
@@ -30,7 +30,7 @@ struct dp_mlp_dev {
     float b2[DP_MLP_H];
     float w3[2][DP_MLP_H];
     float b3[2];
-    float x_mean, x_inv_scale, u_scale, f_scale;
+    float x_mean, x_inv_scale, u_scale, f_scale;  // f_scale scales f r
     float pad[2];
     // W2 as ready-made B fragments: [k-step 4][n-tile 8][lane 32][2 regs]
     uint32_t w2frag[4 * 8 * 32 * 2];

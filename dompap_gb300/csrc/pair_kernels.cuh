@@ -27,6 +27,13 @@
 //   DP_PMODE        0 constant sigma/epsilon, 1 per-type table, 2 dense (N, N) matrix
 //   DP_SIGMA_ONE    1 when sigma is the constant 1 (the division is skipped)
 //   DP_EPS_ONE      1 when epsilon is the constant 1
+//   DP_FF           1 in the float64-parity mode: pair arithmetic in double-float
+//                   (dp_ff.cuh) on the exact 64-bit fixed-point displacement; the
+//                   cut decision within float rounding of r_cut and positions not
+//                   yet wrapped into the box take the float64 path
+#ifndef DP_FF
+#define DP_FF 0
+#endif
 
 #ifndef DP_DIM
 #error "DP_DIM must be defined"
@@ -71,6 +78,23 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
 #if !(DP_REAL_IS_FLOAT)
 #pragma unroll
     for (int k = 0; k < D; ++k) xi[k] = a.pos[k * n + i];
+#endif
+#if DP_FF
+    typedef typename dp_fixed64_t<D>::type fx_t;
+    const fx_t* __restrict__ p64 = (const fx_t*)a.pos64;
+    unsigned long long Xi[D];
+    dp_fixed64_unpack<D>(p64[i], Xi);
+    dpff U[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) U[k] = dpff(a.unit64_hi[k], a.unit64_lo[k]);
+    const bool ff_ok = a.status->far == 0;  // single-shift image == nearest image
+    const float rcut_f = (float)a.rcut;
+    const bool rcut_finite = isfinite(a.rcut);
+    dpff facc[D];
+    dpff sacc;
+#if DP_PMODE == 0
+    const dpff sig_c(a.sigma), isig_c(a.inv_sigma), eps_c(a.epsilon);
+#endif
 #endif
     int ti = 0;
 #if DP_PMODE == 1
@@ -122,6 +146,67 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
             acc_s += (double)(e * dp_pair_c<float>(s, sinv) + (float)(D - 1) * (-e * dp_pair_f<float>(s, sinv)) * rinv);
         }
 #else
+#if DP_FF
+        if (ff_ok) {
+            // double-float pair arithmetic on the exact fixed-point displacement
+            unsigned long long Xj[D];
+            dp_fixed64_unpack<D>(p64[j], Xj);
+            dpff d[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) d[k] = dpff_from_ll((long long)(Xi[k] - Xj[k])) * U[k];
+            dpff q = d[0] * d[0];
+#pragma unroll
+            for (int k = 1; k < D; ++k) q = q + d[k] * d[k];
+            const dpff rinv = dpff_rsqrt(q);
+            const dpff r = q * rinv;
+#if DP_PMODE == 0
+            const dpff fsig = sig_c, fisig = isig_c, feps = eps_c;
+#elif DP_PMODE == 1
+            const int tj = __ldg(a.types + j);
+            const float2* tri = a.ff_tab + 3 * (ti * a.ntypes + tj);
+            const float2 t0 = __ldg(tri), t1 = __ldg(tri + 1), t2 = __ldg(tri + 2);
+            const dpff fsig(t0.x, t0.y), fisig(t1.x, t1.y), feps(t2.x, t2.y);
+#else
+            const dpff fsig(sig), fisig(isig), feps(eps);
+#endif
+#if DP_SIGMA_ONE
+            const dpff s = r, sinv = rinv;
+#else
+            const dpff s = r * fisig, sinv = rinv * fsig;
+#endif
+            if (rcut_finite && fabsf(s.hi - rcut_f) <= 1e-5f * rcut_f) {
+                // within float rounding of r_cut: the reference's float64 decision
+                double dd[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) dd[k] = dp_min_image(a.pos[k * n + i] - __ldg(a.pos + k * n + j), a.box[k]);
+                const double r64 = sqrt(dp_sqsum_exact<D>(dd));
+#if DP_SIGMA_ONE
+                if (r64 > a.rcut) continue;
+#else
+                if (r64 / sig > a.rcut) continue;
+#endif
+            } else if (s.hi > rcut_f) {
+                continue;
+            }
+            if (ACC == DP_ACC_FORCE) {
+#if DP_EPS_ONE
+                const dpff g = dp_pair_f<dpff>(s, sinv) * rinv;
+#else
+                const dpff g = feps * dp_pair_f<dpff>(s, sinv) * rinv;
+#endif
+#pragma unroll
+                for (int k = 0; k < D; ++k) facc[k] = facc[k] + g * d[k];
+            } else if (ACC == DP_ACC_ENERGY) {
+                sacc = sacc + feps * dp_pair_u<dpff>(s, sinv);
+            } else if (ACC == DP_ACC_VIRIAL) {
+                sacc = sacc + feps * dp_pair_f<dpff>(s, sinv) * r;
+            } else {
+                const dpff sf = feps * dp_pair_f<dpff>(s, sinv);
+                sacc = sacc + feps * dp_pair_c<dpff>(s, sinv) - dpff(D - 1) * sf * rinv;
+            }
+            continue;
+        }
+#endif
         // FP64 pair arithmetic. d and r^2 follow the reference exactly; 1/r
         // comes from one reciprocal square root (no divisions), and where s
         // lies within a few ulp of r_cut, r = sqrt(r^2) and s = r / sigma are
@@ -168,11 +253,19 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
         }
 #endif
     }
+#if DP_FF
+    if (ACC == DP_ACC_FORCE) {
+#pragma unroll
+        for (int k = 0; k < D; ++k) f[k] = (double)acc_v[k] + facc[k].to_double();
+    }
+    return acc_s + sacc.to_double();
+#else
     if (ACC == DP_ACC_FORCE) {
 #pragma unroll
         for (int k = 0; k < D; ++k) f[k] = (double)acc_v[k];
     }
     return acc_s;
+#endif
 }
 
 // F (SoA float64) for every particle. One thread per particle.
@@ -240,7 +333,7 @@ extern "C" __global__ void dp_eval_pair(const double* s_in, double* u, double* f
 // lock step: each round gathers one listed pair per particle, evaluates the
 // network on the 32 values of s = r^2 as two 16-row tensor-core tiles, sends
 // each row's result back to the lane owning the particle, and adds
-//   f/r = f_cheap(r)/r + (f/r)_nn,   u = u_cheap(r) + u_nn
+//   f/r = f_cheap(r)/r + (f r)_nn / r^2,   u = u_cheap(r) + u_nn
 // for pairs inside r_cut (sigma = epsilon = 1 in this mode).
 template <int ACC>
 __device__ __forceinline__ void dp_mlp_pass(const dp_pair_args& a, const dp_mlp_dev* mg) {
@@ -295,7 +388,7 @@ __device__ __forceinline__ void dp_mlp_pass(const dp_pair_args& a, const dp_mlp_
         if (valid) {
             const float rinv = rsqrtf(q);
             const float r = q * rinv;
-            const float fr = dp_pair_f<float>(r, rinv) * rinv + nn_f * m.f_scale;
+            const float fr = dp_pair_f<float>(r, rinv) * rinv + nn_f * m.f_scale * (rinv * rinv);
             if (ACC == DP_ACC_FORCE) {
 #pragma unroll
                 for (int k = 0; k < D; ++k) f[k] = fmaf(fr, df[k], f[k]);

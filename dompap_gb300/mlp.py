@@ -3,7 +3,9 @@
 A pair potential string is split into *cheap* terms (integer powers of r and
 constants: evaluated exactly by the generated code) and *costly* terms (anything
 with exp, cos, sin, log, non-integer powers, ...). A small network
-1 -> 64 -> 64 -> 2 in s = r^2 learns (u, f/r) of the costly terms; the GPU pair
+1 -> 64 -> 64 -> 2 in s = r^2 learns (u, f r) of the costly terms (f r rather
+than f/r: the pair virial and the long-range forces weigh errors by r^2, so the
+network's error is kept uniform in f r); the GPU pair
 kernels then evaluate the cheap terms in float32 and the network on tensor
 cores (bf16 weights, fp32 accumulation). The network is trained on the GPU by
 the library's own forward/backward kernels (Adam) on samples of the
@@ -78,9 +80,10 @@ class PairSurrogate:
         r = rng.uniform(self.r_min, self.r_cut, size=n_samples)
         u, f = _eval_codegen_fp64(self.costly_str, self.r_cut, r)
         s = r * r
-        fr = f / r
-        self.norm = np.array([s.mean(), 1.0 / s.std(), np.max(np.abs(u)), np.max(np.abs(fr))], dtype=np.float32)
-        targets = np.stack([u / self.norm[2], fr / self.norm[3]], axis=1).astype(np.float32)
+        f_times_r = f * r
+        self.norm = np.array([s.mean(), 1.0 / s.std(), np.max(np.abs(u)), np.max(np.abs(f_times_r))],
+                             dtype=np.float32)
+        targets = np.stack([u / self.norm[2], f_times_r / self.norm[3]], axis=1).astype(np.float32)
         lib = _lib.load()
         h = ctypes.c_void_p()
         _lib.check(lib.dp_mlp_create(ctypes.byref(h)))
@@ -137,8 +140,9 @@ class PairSurrogate:
 
     def costly_terms(self, r: np.ndarray):
         """(u, f/r) of the costly terms predicted by the network."""
-        y = self.network(np.asarray(r, dtype=np.float64) ** 2).astype(np.float64)
-        return y[:, 0] * float(self.norm[2]), y[:, 1] * float(self.norm[3])
+        r = np.asarray(r, dtype=np.float64)
+        y = self.network(r ** 2).astype(np.float64)
+        return y[:, 0] * float(self.norm[2]), y[:, 1] * float(self.norm[3]) / (r * r)
 
     def errors(self, n: int = 200000, seed: int = 1) -> dict:
         """Accuracy against the float64 generated code on fresh samples in
