@@ -554,7 +554,7 @@ __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
             if (NVE) {
                 v = v + c[4] * F;  // make_one_step_leap_frog (dompap/integrator.py:12)
             } else {
-                const double bn = c[3] * (double)z[k];
+                const double bn = c[3] * dp_f2d(z[k]);
                 v = c[0] * v + c[1] * F + c[2] * (a.beta[o] + bn);
                 a.beta[o] = bn;
             }
@@ -1202,6 +1202,15 @@ static void fill_pair_args(const dp_sim* s, dp_pair_args& a, double* out) {
     a.inv_sigma = 1.0 / s->sigma;
     a.epsilon = s->epsilon;
     a.rcut = s->r_cut;
+    a.rcut_f = (float)s->r_cut;
+    a.rcut_finite = std::isfinite(s->r_cut) ? 1 : 0;
+    {
+        const double c3[3] = {a.sigma, a.inv_sigma, a.epsilon};
+        for (int t = 0; t < 3; ++t) {
+            a.ff_const[2 * t] = (float)c3[t];
+            a.ff_const[2 * t + 1] = (float)(c3[t] - (double)(float)c3[t]);
+        }
+    }
     // Pre-filter threshold: a pair is skipped only when its float32 distance,
     // whose error is < 1e-6 relative plus a few L / 2^32, certainly exceeds
     // r_cut * sigma_max.
@@ -2656,6 +2665,7 @@ int dp_batch_last_forces(dp_batch* b, double* forces) {
 // ===========================================================================
 struct dp_mlp {
     float *master = nullptr, *mo = nullptr, *ve = nullptr, *grad = nullptr, *norm = nullptr, *loss = nullptr;
+    unsigned long long* gradfx = nullptr;  // DP_MLP_NPARAM + 1 (the loss last)
     dp_mlp_dev* dev = nullptr;
     float* s = nullptr;
     float2* t = nullptr;
@@ -2683,18 +2693,19 @@ static int mlp_grad_launch(dp_mlp* m, const float* s, const float2* t, const lon
     a.batch = batch;
     a.mdev = m->dev;
     a.master = m->master;
-    a.grad = m->grad;
-    a.loss = m->loss;
+    a.gradfx = m->gradfx;
+    a.lossfx = m->gradfx + DP_MLP_NPARAM;
     a.wf = wf;
     a.inv_batch = 1.0f / (float)batch;
-    CK(cudaMemsetAsync(m->grad, 0, DP_MLP_NPARAM * sizeof(float), m->stream));
-    CK(cudaMemsetAsync(m->loss, 0, sizeof(float), m->stream));
+    CK(cudaMemsetAsync(m->gradfx, 0, (DP_MLP_NPARAM + 1) * sizeof(unsigned long long), m->stream));
     const long long tiles = (batch + 15) / 16;
     const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>((tiles + 7) / 8, 152LL * 4));
     if (accurate)
         k_mlp_grad<true><<<grid, 256, DP_MLP_GRAD_SMEM, m->stream>>>(a);
     else
         k_mlp_grad<false><<<grid, 256, DP_MLP_GRAD_SMEM, m->stream>>>(a);
+    k_mlp_grad_finish<<<grid_for(DP_MLP_NPARAM, kBlock), kBlock, 0, m->stream>>>(a.gradfx, a.lossfx, m->grad,
+                                                                                   m->loss);
     CK(cudaGetLastError());
     return DP_OK;
 }
@@ -2708,7 +2719,8 @@ int dp_mlp_create(dp_mlp** out) {
     int rc = DP_OK;
     if ((rc = dalloc_t(&m->master, DP_MLP_NPARAM)) || (rc = dalloc_t(&m->mo, DP_MLP_NPARAM)) ||
         (rc = dalloc_t(&m->ve, DP_MLP_NPARAM)) || (rc = dalloc_t(&m->grad, DP_MLP_NPARAM)) ||
-        (rc = dalloc_t(&m->norm, 4)) || (rc = dalloc_t(&m->loss, 1)) || (rc = dalloc_t(&m->dev, 1))) {
+        (rc = dalloc_t(&m->norm, 4)) || (rc = dalloc_t(&m->loss, 1)) || (rc = dalloc_t(&m->dev, 1)) ||
+        (rc = dalloc_t(&m->gradfx, DP_MLP_NPARAM + 1))) {
         dp_mlp_destroy(m);
         return rc;
     }
@@ -2730,7 +2742,8 @@ int dp_mlp_create(dp_mlp** out) {
 int dp_mlp_destroy(dp_mlp* m) {
     if (!m) return DP_OK;
     if (m->stream) cudaStreamSynchronize(m->stream);
-    void* bufs[] = {m->master, m->mo, m->ve, m->grad, m->norm, m->loss, m->dev, m->s, m->t, m->idx, m->losses};
+    void* bufs[] = {m->master, m->mo, m->ve, m->grad, m->norm, m->loss, m->dev, m->s, m->t, m->idx, m->losses,
+                    m->gradfx};
     for (void* p : bufs)
         if (p) cudaFree(p);
     if (m->stream) cudaStreamDestroy(m->stream);

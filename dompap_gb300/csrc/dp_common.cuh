@@ -56,6 +56,9 @@ struct dp_pair_args {
     double epsilon;          // DP_PMODE == 0
     double rcut;             // r_cut in units of sigma
     float cut2f;             // pre-filter: skip a pair when its float32 r^2 exceeds this
+    float rcut_f;            // (float) rcut
+    int rcut_finite;
+    float ff_const[6];       // DP_PMODE == 0: sigma, 1/sigma, epsilon as double-float pairs
     int pad1;
 };
 
@@ -172,7 +175,45 @@ __device__ __forceinline__ ulonglong4 dp_fixed64_pack<4>(const unsigned long lon
 // Both fixed-point forms of one coordinate from the float64 product
 // p = x 2^64 / L: the 64-bit one and its upper 32 bits (the shadow). The
 // coordinate must lie in [0, L); a product rounded up to 2^64 saturates.
-__device__ __forceinline__ unsigned long long dp_fixed64_of(double p) { return __double2ull_rd(p); }
+// floor(p) from the bit pattern (integer shifts; this GPU issues float64
+// conversion instructions at the float64 rate): p < 1 and negative p give 0,
+// p >= 2^64 saturates.
+__device__ __forceinline__ unsigned long long dp_fixed64_of(double p) {
+    const long long b = __double_as_longlong(p);
+    const int e = (int)((b >> 52) & 0x7FF) - 1023;
+    if (b < 0 || e < 0) return 0ull;
+    if (e >= 64) return ~0ull;
+    const unsigned long long m = ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    return e >= 52 ? m << (e - 52) : m >> (52 - e);
+}
+
+// x is neither infinite nor NaN (integer test of the exponent field).
+__device__ __forceinline__ bool dp_isfinite_bits(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7FF0000000000000ull) != 0x7FF0000000000000ull;
+}
+
+// Integer m with -2^22 <= m < 2^22 as a float, exactly: one integer add to
+// the bit pattern of 1.5 * 2^23 and one float subtraction.
+__device__ __forceinline__ float dp_small_int(int m) { return __int_as_float(0x4B400000 + m) - 12582912.0f; }
+
+// int32 -> float rounded to nearest, on the integer and FMA pipes (this GPU
+// issues conversion instructions at the float64 rate): n = h 2^16 + l with
+// h = n >> 16 and l = n & 0xFFFF exact floats; the FMA rounds h 2^16 + l once.
+__device__ __forceinline__ float dp_i2f(int n) {
+    return fmaf(dp_small_int(n >> 16), 65536.0f, dp_small_int(n & 0xFFFF));
+}
+
+// float -> double by moving the bits (sign, exponent rebiased, mantissa);
+// subnormals, infinities and NaN take the conversion instruction.
+__device__ __forceinline__ double dp_f2d(float z) {
+    const uint32_t b = __float_as_uint(z);
+    const uint32_t e = (b >> 23) & 0xFFu;
+    if ((b & 0x7FFFFFFFu) == 0u) return __longlong_as_double((long long)((unsigned long long)b << 32));
+    if (e == 0u || e == 0xFFu) return (double)z;
+    return __longlong_as_double((long long)(((unsigned long long)(b >> 31) << 63) |
+                                            ((unsigned long long)(e + (1023u - 127u)) << 52) |
+                                            ((unsigned long long)(b & 0x7FFFFFu) << 29)));
+}
 
 template <int D>
 struct dp_shadow_t;
@@ -232,8 +273,7 @@ __device__ __forceinline__ float dp_shadow_q(const uint32_t* ui, const uint32_t*
     float q = 0.0f;
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-        const int n = (int)(ui[k] - uj[k]);
-        df[k] = (float)n * unit[k];
+        df[k] = dp_i2f((int)(ui[k] - uj[k])) * unit[k];
         q = fmaf(df[k], df[k], q);
     }
     return q;

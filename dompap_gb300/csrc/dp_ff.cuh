@@ -31,11 +31,13 @@ __device__ __forceinline__ dpff dpff_two_sum(float a, float b) {
     return dpff(s, (a - (s - bb)) + (b - bb));
 }
 
+// Dekker's addition: absolute error below ~2^-47 (|x| + |y|), relative
+// 2^-47 for operands of one sign; the pair sums need no more (their float64
+// counterparts carry 2^-53 (|x| + |y|)), at about half the instructions of
+// the sign-robust form.
 __device__ __forceinline__ dpff operator+(dpff x, dpff y) {
     const dpff s = dpff_two_sum(x.hi, y.hi);
-    const dpff t = dpff_two_sum(x.lo, y.lo);
-    const dpff u = dpff_quick_two_sum(s.hi, s.lo + t.hi);
-    return dpff_quick_two_sum(u.hi, u.lo + t.lo);
+    return dpff_quick_two_sum(s.hi, s.lo + (x.lo + y.lo));
 }
 
 __device__ __forceinline__ dpff operator-(dpff x) { return dpff(-x.hi, -x.lo); }
@@ -81,12 +83,36 @@ __device__ __forceinline__ dpff dpff_rsqrt(dpff q) {
     return dpff(y0, 0.0f) + dpff_mul_f(e, 0.5f * y0);
 }
 
-// Exact int64 -> double-float (hi = nearest float, lo = rounded remainder).
-__device__ __forceinline__ dpff dpff_from_ll(long long v) {
-    const float hi = __ll2float_rn(v);
-    const long long rem = v - __float2ll_rn(hi);
-    return dpff(hi, __ll2float_rn(rem));
+__device__ __forceinline__ dpff dpff_add_f(dpff x, float b) {
+    const dpff s = dpff_two_sum(x.hi, b);
+    return dpff_quick_two_sum(s.hi, s.lo + x.lo);
 }
+
+// int64 -> double-float (rounded to ~48 bits) without 64-bit conversion
+// instructions: v = a 2^42 + b 2^20 + c with a in [-2^21, 2^21), b < 2^22,
+// c < 2^20, each piece an exact float; a 2^42 + b 2^20 has at most 44
+// significant bits, so its TwoSum is exact, and c is added last.
+__device__ __forceinline__ dpff dpff_from_ll(long long v) {
+    const int a = (int)(v >> 42);
+    const int b = (int)(((unsigned long long)v >> 20) & 0x3FFFFFull);
+    const int c = (int)((unsigned long long)v & 0xFFFFFull);
+    const float fa = dp_small_int(a) * 4398046511104.0f;  // 2^42
+    const float fb = dp_small_int(b) * 1048576.0f;        // 2^20
+    return dpff_add_f(dpff_two_sum(fa, fb), dp_small_int(c));
+}
+
+// Compensated accumulation s += v (cascaded summation in the manner of
+// Neumaier): s.hi carries the running float sum, s.lo collects the exact
+// rounding errors of s.hi and the low parts of the addends, unnormalised;
+// the value is s.hi + s.lo.
+__device__ __forceinline__ void dpff_accumulate(dpff& s, dpff v) {
+    const dpff t = dpff_two_sum(s.hi, v.hi);
+    s.hi = t.hi;
+    s.lo += t.lo + v.lo;
+}
+
+// hi + lo in float64 with the two widenings done on bit patterns.
+__device__ __forceinline__ double dpff_to_double(dpff x) { return dp_f2d(x.hi) + dp_f2d(x.lo); }
 
 // Functions without a double-float form go through float64.
 #define DPFF_VIA_DOUBLE(fn)                                                                    \

@@ -3,9 +3,15 @@
 //
 // Parameters (fp32 masters, flat, DP_MLP_NPARAM): w1[64], b1[64],
 // W2[64][64] (row = output unit), b2[64], W3[2][64], b3[2]. The forward pass
-// uses bf16-rounded weights (quantisation-aware training), biases in fp32.
-// Loss per sample: (y0 - t0)^2 + wf (y1 - t1)^2, averaged over the batch.
+// uses bf16-rounded W2 (the tensor-core operand; quantisation-aware
+// training) and fp32 biases; w1 and W3 feed float32 FMAs and stay fp32 unless
+// DP_MLP_SCALAR_BF16 is 1. Loss per sample: (y0 - t0)^2 + wf (y1 - t1)^2,
+// averaged over the batch.
 #pragma once
+
+#ifndef DP_MLP_SCALAR_BF16
+#define DP_MLP_SCALAR_BF16 0
+#endif
 
 #define DP_MLP_NPARAM (64 + 64 + 64 * 64 + 64 + 2 * 64 + 2)
 #define DP_MLP_OFF_W1 0
@@ -24,11 +30,12 @@ __device__ __forceinline__ float dp_round_bf16(float v) {
 __global__ void k_mlp_pack(const float* __restrict__ p, const float* __restrict__ norm, dp_mlp_dev* m) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < 64) {
-        m->w1[t] = dp_round_bf16(p[DP_MLP_OFF_W1 + t]);
+        const float w1 = p[DP_MLP_OFF_W1 + t], w30 = p[DP_MLP_OFF_W3 + t], w31 = p[DP_MLP_OFF_W3 + 64 + t];
+        m->w1[t] = DP_MLP_SCALAR_BF16 ? dp_round_bf16(w1) : w1;
         m->b1[t] = p[DP_MLP_OFF_B1 + t];
         m->b2[t] = p[DP_MLP_OFF_B2 + t];
-        m->w3[0][t] = dp_round_bf16(p[DP_MLP_OFF_W3 + t]);
-        m->w3[1][t] = dp_round_bf16(p[DP_MLP_OFF_W3 + 64 + t]);
+        m->w3[0][t] = DP_MLP_SCALAR_BF16 ? dp_round_bf16(w30) : w30;
+        m->w3[1][t] = DP_MLP_SCALAR_BF16 ? dp_round_bf16(w31) : w31;
     }
     if (t < 2) m->b3[t] = p[DP_MLP_OFF_B3 + t];
     if (t == 0) {
@@ -77,45 +84,65 @@ __global__ void __launch_bounds__(256) k_mlp_eval(const float* __restrict__ s, l
 
 // Gradient of the batch loss: forward on tensor cores (as inference), the
 // backward GEMMs dW2 = dZ2^T H1 and dH1 = dZ2 W2 as bf16 mma.sync with fp32
-// accumulation; per-CTA sums in shared memory, then one atomicAdd per
-// parameter into grad[]. Samples: s[idx[b]] (idx null: b) for b < batch.
+// accumulation. Every sum across warps and CTAs is taken in 64-bit fixed
+// point (integer adds are exact, so the result does not depend on the order
+// of the atomics and training is reproducible for a seed): per-CTA sums in
+// shared memory, then one atomic per parameter into gradfx[];
+// k_mlp_grad_finish turns them into float. Samples: s[idx[b]] (idx null: b)
+// for b < batch.
 struct MlpTrainArgs {
     const float* s;
     const float2* t;
     const long long* idx;
     long long batch;
     const dp_mlp_dev* mdev;
-    const float* master;  // fp32 W2 for the backward product
-    float* grad;          // DP_MLP_NPARAM
-    float* loss;          // sum of per-sample losses (atomic)
+    const float* master;               // fp32 W2 for the backward product
+    unsigned long long* gradfx;        // DP_MLP_NPARAM, fixed point 2^DP_MLP_GRAD_FX_BITS
+    unsigned long long* lossfx;        // sum of per-sample losses, fixed point 2^DP_MLP_LOSS_FX_BITS
     float wf;
     float inv_batch;
 };
 
+#define DP_MLP_GRAD_FX_BITS 36
+#define DP_MLP_LOSS_FX_BITS 32
+
+// v as a two's-complement fixed-point integer 2^BITS v (saturating; a
+// gradient beyond 2^(63-BITS) means the training has diverged anyway).
+template <int BITS>
+__device__ __forceinline__ unsigned long long dp_fx(float v) {
+    return (unsigned long long)__float2ll_rn(v * (float)(1ull << BITS));
+}
+
+template <int BITS>
+__device__ __forceinline__ void dp_fx_add(unsigned long long* p, float v) {
+    atomicAdd(p, dp_fx<BITS>(v));
+}
+
 // dynamic shared memory of k_mlp_grad (bytes)
-#define DP_MLP_GRAD_SMEM (64 * 64 * 4 + 64 * 64 * 2 + 8 * 2 * 16 * 64 * 2)
+#define DP_MLP_GRAD_SMEM (64 * 64 * 8 + 64 * 64 * 2 + 8 * 2 * 16 * 64 * 2)
 
 template <bool ACCURATE>
 __global__ void __launch_bounds__(256) k_mlp_grad(MlpTrainArgs a) {
     __shared__ dp_mlp_dev m;
-    __shared__ float gsmall[64 * 4 + 128 + 2 + 1];  // gw1, gb1, gb2, (unused), gw3, gb3, loss
+    __shared__ unsigned long long gsmall[64 * 4 + 128 + 2 + 1];  // gw1, gb1, gb2, (unused), gw3, gb3, loss
     extern __shared__ __align__(16) unsigned char dp_grad_smem[];
-    float* gW2 = (float*)dp_grad_smem;                                       // [n][k] fp32
+    unsigned long long* gW2 = (unsigned long long*)dp_grad_smem;            // [n][k] fixed point
     __nv_bfloat16* w2s = (__nv_bfloat16*)(gW2 + 64 * 64);                   // [n][k]
     __nv_bfloat16* stage = w2s + 64 * 64;                                    // [warp][2][16 * 64]
     dp_mlp_load(&m, a.mdev);
     for (int t = threadIdx.x; t < 64 * 64; t += blockDim.x) {
-        gW2[t] = 0.f;
+        gW2[t] = 0ull;
         w2s[t] = __float2bfloat16_rn(a.master[DP_MLP_OFF_W2 + t]);
     }
-    for (int t = threadIdx.x; t < 64 * 4 + 128 + 3; t += blockDim.x) gsmall[t] = 0.f;
+    for (int t = threadIdx.x; t < 64 * 4 + 128 + 3; t += blockDim.x) gsmall[t] = 0ull;
     __syncthreads();
-    float* gw1 = gsmall;
-    float* gb1 = gsmall + 64;
-    float* gb2 = gsmall + 128;
-    float* gw3 = gsmall + 256;
-    float* gb3 = gsmall + 256 + 128;
-    float* gloss = gsmall + 256 + 130;
+    constexpr int GB = DP_MLP_GRAD_FX_BITS;
+    unsigned long long* gw1 = gsmall;
+    unsigned long long* gb1 = gsmall + 64;
+    unsigned long long* gb2 = gsmall + 128;
+    unsigned long long* gw3 = gsmall + 256;
+    unsigned long long* gb3 = gsmall + 256 + 128;
+    unsigned long long* gloss = gsmall + 256 + 130;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, c = 2 * (lane & 3);
     __nv_bfloat16* sdz = stage + (warp * 2 + 0) * 16 * 64;
     __nv_bfloat16* sh1 = stage + (warp * 2 + 1) * 16 * 64;
@@ -156,7 +183,8 @@ __global__ void __launch_bounds__(256) k_mlp_grad(MlpTrainArgs a) {
         const float2 t0 = v0 ? a.t[i0] : make_float2(0.f, 0.f), t1 = v1 ? a.t[i1] : make_float2(0.f, 0.f);
         const float e00 = v0 ? p00 + m.b3[0] - t0.x : 0.f, e01 = v0 ? p01 + m.b3[1] - t0.y : 0.f;
         const float e10 = v1 ? p10 + m.b3[0] - t1.x : 0.f, e11 = v1 ? p11 + m.b3[1] - t1.y : 0.f;
-        if ((lane & 3) == 0) atomicAdd(gloss, e00 * e00 + a.wf * e01 * e01 + e10 * e10 + a.wf * e11 * e11);
+        if ((lane & 3) == 0)
+            dp_fx_add<DP_MLP_LOSS_FX_BITS>(gloss, e00 * e00 + a.wf * e01 * e01 + e10 * e10 + a.wf * e11 * e11);
         // dL/dy (mean over the batch)
         const float d00 = 2.f * e00 * a.inv_batch, d01 = 2.f * a.wf * e01 * a.inv_batch;
         const float d10 = 2.f * e10 * a.inv_batch, d11 = 2.f * a.wf * e11 * a.inv_batch;
@@ -168,8 +196,8 @@ __global__ void __launch_bounds__(256) k_mlp_grad(MlpTrainArgs a) {
             sb31 += __shfl_xor_sync(0xffffffffu, sb31, o);
         }
         if (lane == 0) {
-            atomicAdd(gb3, sb30);
-            atomicAdd(gb3 + 1, sb31);
+            dp_fx_add<GB>(gb3, sb30);
+            dp_fx_add<GB>(gb3 + 1, sb31);
         }
         // dz2 = (dy0 w3[0] + dy1 w3[1]) * act'(z2); gw3, gb2 partial sums
 #pragma unroll
@@ -190,9 +218,9 @@ __global__ void __launch_bounds__(256) k_mlp_grad(MlpTrainArgs a) {
                     gbb += __shfl_xor_sync(0xffffffffu, gbb, o);
                 }
                 if (g == 0) {
-                    atomicAdd(gw3 + col, gw30);
-                    atomicAdd(gw3 + 64 + col, gw31);
-                    atomicAdd(gb2 + col, gbb);
+                    dp_fx_add<GB>(gw3 + col, gw30);
+                    dp_fx_add<GB>(gw3 + 64 + col, gw31);
+                    dp_fx_add<GB>(gb2 + col, gbb);
                 }
                 sdz[g * 64 + col] = __float2bfloat16_rn(dzg);
                 sdz[(g + 8) * 64 + col] = __float2bfloat16_rn(dzg8);
@@ -228,10 +256,10 @@ __global__ void __launch_bounds__(256) k_mlp_grad(MlpTrainArgs a) {
                 float acc[4] = {0.f, 0.f, 0.f, 0.f};
                 dp_mma_bf16(acc, af, bb0, bb1);
                 const int row = mt * 16 + g, col = nt * 8 + c;
-                atomicAdd(gW2 + row * 64 + col, acc[0]);
-                atomicAdd(gW2 + row * 64 + col + 1, acc[1]);
-                atomicAdd(gW2 + (row + 8) * 64 + col, acc[2]);
-                atomicAdd(gW2 + (row + 8) * 64 + col + 1, acc[3]);
+                dp_fx_add<GB>(gW2 + row * 64 + col, acc[0]);
+                dp_fx_add<GB>(gW2 + row * 64 + col + 1, acc[1]);
+                dp_fx_add<GB>(gW2 + (row + 8) * 64 + col, acc[2]);
+                dp_fx_add<GB>(gW2 + (row + 8) * 64 + col + 1, acc[3]);
             }
         }
         // dh1[row][k] = sum_n dz2[row][n] W2[n][k]: M = rows, N = k, K = n (4 k-steps)
@@ -271,23 +299,32 @@ __global__ void __launch_bounds__(256) k_mlp_grad(MlpTrainArgs a) {
                     gb += __shfl_xor_sync(0xffffffffu, gb, o);
                 }
                 if (g == 0) {
-                    atomicAdd(gw1 + k, gw);
-                    atomicAdd(gb1 + k, gb);
+                    dp_fx_add<GB>(gw1 + k, gw);
+                    dp_fx_add<GB>(gb1 + k, gb);
                 }
             }
         __syncwarp();
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < 64 * 64; t += blockDim.x) atomicAdd(a.grad + DP_MLP_OFF_W2 + t, gW2[t]);
+    unsigned long long* G = a.gradfx;
+    for (int t = threadIdx.x; t < 64 * 64; t += blockDim.x) atomicAdd(G + DP_MLP_OFF_W2 + t, gW2[t]);
     for (int t = threadIdx.x; t < 64; t += blockDim.x) {
-        atomicAdd(a.grad + DP_MLP_OFF_W1 + t, gw1[t]);
-        atomicAdd(a.grad + DP_MLP_OFF_B1 + t, gb1[t]);
-        atomicAdd(a.grad + DP_MLP_OFF_B2 + t, gb2[t]);
-        atomicAdd(a.grad + DP_MLP_OFF_W3 + t, gw3[t]);
-        atomicAdd(a.grad + DP_MLP_OFF_W3 + 64 + t, gw3[64 + t]);
+        atomicAdd(G + DP_MLP_OFF_W1 + t, gw1[t]);
+        atomicAdd(G + DP_MLP_OFF_B1 + t, gb1[t]);
+        atomicAdd(G + DP_MLP_OFF_B2 + t, gb2[t]);
+        atomicAdd(G + DP_MLP_OFF_W3 + t, gw3[t]);
+        atomicAdd(G + DP_MLP_OFF_W3 + 64 + t, gw3[64 + t]);
     }
-    if (threadIdx.x < 2) atomicAdd(a.grad + DP_MLP_OFF_B3 + threadIdx.x, gb3[threadIdx.x]);
-    if (threadIdx.x == 0) atomicAdd(a.loss, *gloss);
+    if (threadIdx.x < 2) atomicAdd(G + DP_MLP_OFF_B3 + threadIdx.x, gb3[threadIdx.x]);
+    if (threadIdx.x == 0) atomicAdd(a.lossfx, *gloss);
+}
+
+// Fixed-point sums -> float gradient and loss.
+__global__ void k_mlp_grad_finish(const unsigned long long* __restrict__ gradfx,
+                                  const unsigned long long* __restrict__ lossfx, float* grad, float* loss) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < DP_MLP_NPARAM) grad[t] = (float)((double)(long long)gradfx[t] * (1.0 / (double)(1ull << DP_MLP_GRAD_FX_BITS)));
+    if (t == 0) *loss = (float)((double)(long long)*lossfx * (1.0 / (double)(1ull << DP_MLP_LOSS_FX_BITS)));
 }
 
 // Adam (Kingma & Ba 2015) on the fp32 masters.

@@ -67,35 +67,21 @@ enum { DP_ACC_FORCE = 0, DP_ACC_ENERGY = 1, DP_ACC_VIRIAL = 2, DP_ACC_LAPLACE = 
 
 // Per-particle neighbour loop. Returns the scalar sum (energy / virial /
 // Laplacian) and, for DP_ACC_FORCE, the force vector in f[].
+//
+// Float64-parity mode (DP_FF): a pair is evaluated in double-float on the
+// exact 64-bit fixed-point displacement, with no float64 instruction in the
+// loop (this GPU runs float64 at 1/64 of the float32 rate). Pairs whose
+// scaled distance lies within float rounding of r_cut, and every pair while
+// some position is far outside the box, take the float64 path of the
+// reference instead (its min-image displacement, cut decision and pair
+// terms).
 template <int ACC>
 __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long long i, double* f) {
     constexpr int D = DP_DIM;
     const long long n = a.n;
     const shadow_t* __restrict__ sh = (const shadow_t*)a.shadow;
     uint32_t ui[D];
-    dp_shadow_unpack<D>(sh[i], ui);
     double xi[D];
-#if !(DP_REAL_IS_FLOAT)
-#pragma unroll
-    for (int k = 0; k < D; ++k) xi[k] = a.pos[k * n + i];
-#endif
-#if DP_FF
-    typedef typename dp_fixed64_t<D>::type fx_t;
-    const fx_t* __restrict__ p64 = (const fx_t*)a.pos64;
-    unsigned long long Xi[D];
-    dp_fixed64_unpack<D>(p64[i], Xi);
-    dpff U[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) U[k] = dpff(a.unit64_hi[k], a.unit64_lo[k]);
-    const bool ff_ok = a.status->far == 0;  // single-shift image == nearest image
-    const float rcut_f = (float)a.rcut;
-    const bool rcut_finite = isfinite(a.rcut);
-    dpff facc[D];
-    dpff sacc;
-#if DP_PMODE == 0
-    const dpff sig_c(a.sigma), isig_c(a.inv_sigma), eps_c(a.epsilon);
-#endif
-#endif
     int ti = 0;
 #if DP_PMODE == 1
     ti = a.types[i];
@@ -104,6 +90,40 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
 #pragma unroll
     for (int k = 0; k < D; ++k) acc_v[k] = real_t(0);
     double acc_s = 0.0;
+#if DP_FF
+    typedef typename dp_fixed64_t<D>::type fx_t;
+    const fx_t* __restrict__ p64 = (const fx_t*)a.pos64;
+    const bool ff_ok = a.status->far == 0;  // single-shift image == nearest image
+    unsigned long long Xi[D];
+    dpff U[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) U[k] = dpff(a.unit64_hi[k], a.unit64_lo[k]);
+    if (ff_ok) {
+        // the pre-filter runs on the upper words of the 64-bit fixed point
+        dp_fixed64_unpack<D>(p64[i], Xi);
+#pragma unroll
+        for (int k = 0; k < D; ++k) ui[k] = (uint32_t)(Xi[k] >> 32);
+    } else {
+        dp_shadow_unpack<D>(sh[i], ui);
+#pragma unroll
+        for (int k = 0; k < D; ++k) xi[k] = a.pos[k * n + i];
+    }
+    const float rcut_f = a.rcut_f;
+    const bool rcut_finite = a.rcut_finite != 0;
+    dpff facc[D];  // compensated sums (dpff_accumulate)
+    dpff sacc;
+    bool used64 = false;
+#if DP_PMODE == 0
+    const dpff sig_c(a.ff_const[0], a.ff_const[1]), isig_c(a.ff_const[2], a.ff_const[3]),
+        eps_c(a.ff_const[4], a.ff_const[5]);
+#endif
+#else
+    dp_shadow_unpack<D>(sh[i], ui);
+#if !(DP_REAL_IS_FLOAT)
+#pragma unroll
+    for (int k = 0; k < D; ++k) xi[k] = a.pos[k * n + i];
+#endif
+#endif
     const int c = a.cnt[i];
     const int32_t* __restrict__ row = a.nl + i;
     for (int kk = 0; kk < c; ++kk) {
@@ -112,13 +132,26 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
         // sigma(n, m), epsilon(n, m) (dompap/potential.py:265-278)
         if (ACC == DP_ACC_VIRIAL && j <= i) continue;
         uint32_t uj[D];
+#if DP_FF
+        // one gather per neighbour: the 64-bit fixed point, whose upper words
+        // are the shadow
+        unsigned long long Xj[D];
+        if (ff_ok) {
+            dp_fixed64_unpack<D>(p64[j], Xj);
+#pragma unroll
+            for (int k = 0; k < D; ++k) uj[k] = (uint32_t)(Xj[k] >> 32);
+        } else {
+            dp_shadow_unpack<D>(__ldg(sh + j), uj);
+        }
+#else
         dp_shadow_unpack<D>(__ldg(sh + j), uj);
+#endif
         float df[D];
         const float qf = dp_shadow_q<D>(ui, uj, a.unit, df);
         if (qf > a.cut2f) continue;  // certainly beyond r_cut * sigma_max
+#if DP_REAL_IS_FLOAT
         double sig, isig, eps;
         dp_pair_params(a, i, ti, j, sig, isig, eps);
-#if DP_REAL_IS_FLOAT
         // FP32 pair arithmetic on the fixed-point displacement.
         const float rinv = rsqrtf(qf);
         const float r = qf * rinv;
@@ -149,8 +182,6 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
 #if DP_FF
         if (ff_ok) {
             // double-float pair arithmetic on the exact fixed-point displacement
-            unsigned long long Xj[D];
-            dp_fixed64_unpack<D>(p64[j], Xj);
             dpff d[D];
 #pragma unroll
             for (int k = 0; k < D; ++k) d[k] = dpff_from_ll((long long)(Xi[k] - Xj[k])) * U[k];
@@ -167,6 +198,8 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
             const float2 t0 = __ldg(tri), t1 = __ldg(tri + 1), t2 = __ldg(tri + 2);
             const dpff fsig(t0.x, t0.y), fisig(t1.x, t1.y), feps(t2.x, t2.y);
 #else
+            double sig, isig, eps;
+            dp_pair_params(a, i, ti, j, sig, isig, eps);
             const dpff fsig(sig), fisig(isig), feps(eps);
 #endif
 #if DP_SIGMA_ONE
@@ -174,44 +207,39 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
 #else
             const dpff s = r * fisig, sinv = rinv * fsig;
 #endif
-            if (rcut_finite && fabsf(s.hi - rcut_f) <= 1e-5f * rcut_f) {
-                // within float rounding of r_cut: the reference's float64 decision
-                double dd[D];
-#pragma unroll
-                for (int k = 0; k < D; ++k) dd[k] = dp_min_image(a.pos[k * n + i] - __ldg(a.pos + k * n + j), a.box[k]);
-                const double r64 = sqrt(dp_sqsum_exact<D>(dd));
-#if DP_SIGMA_ONE
-                if (r64 > a.rcut) continue;
+            if (!(rcut_finite && fabsf(s.hi - rcut_f) <= 1e-5f * rcut_f)) {
+                if (s.hi > rcut_f) continue;
+                if (ACC == DP_ACC_FORCE) {
+#if DP_EPS_ONE
+                    const dpff g = dp_pair_f<dpff>(s, sinv) * rinv;
 #else
-                if (r64 / sig > a.rcut) continue;
+                    const dpff g = feps * dp_pair_f<dpff>(s, sinv) * rinv;
 #endif
-            } else if (s.hi > rcut_f) {
+#pragma unroll
+                    for (int k = 0; k < D; ++k) dpff_accumulate(facc[k], g * d[k]);
+                } else if (ACC == DP_ACC_ENERGY) {
+                    dpff_accumulate(sacc, feps * dp_pair_u<dpff>(s, sinv));
+                } else if (ACC == DP_ACC_VIRIAL) {
+                    dpff_accumulate(sacc, feps * dp_pair_f<dpff>(s, sinv) * r);
+                } else {
+                    const dpff sf = feps * dp_pair_f<dpff>(s, sinv);
+                    dpff_accumulate(sacc, feps * dp_pair_c<dpff>(s, sinv) - dpff(D - 1) * sf * rinv);
+                }
                 continue;
             }
-            if (ACC == DP_ACC_FORCE) {
-#if DP_EPS_ONE
-                const dpff g = dp_pair_f<dpff>(s, sinv) * rinv;
-#else
-                const dpff g = feps * dp_pair_f<dpff>(s, sinv) * rinv;
-#endif
+            // within float rounding of r_cut: the float64 path below
 #pragma unroll
-                for (int k = 0; k < D; ++k) facc[k] = facc[k] + g * d[k];
-            } else if (ACC == DP_ACC_ENERGY) {
-                sacc = sacc + feps * dp_pair_u<dpff>(s, sinv);
-            } else if (ACC == DP_ACC_VIRIAL) {
-                sacc = sacc + feps * dp_pair_f<dpff>(s, sinv) * r;
-            } else {
-                const dpff sf = feps * dp_pair_f<dpff>(s, sinv);
-                sacc = sacc + feps * dp_pair_c<dpff>(s, sinv) - dpff(D - 1) * sf * rinv;
-            }
-            continue;
+            for (int k = 0; k < D; ++k) xi[k] = a.pos[k * n + i];
         }
+        used64 = true;
 #endif
         // FP64 pair arithmetic. d and r^2 follow the reference exactly; 1/r
         // comes from one reciprocal square root (no divisions), and where s
         // lies within a few ulp of r_cut, r = sqrt(r^2) and s = r / sigma are
         // recomputed with IEEE operations so the cut decision is the
         // reference's.
+        double sig, isig, eps;
+        dp_pair_params(a, i, ti, j, sig, isig, eps);
         double d[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) d[k] = dp_min_image(xi[k] - __ldg(a.pos + k * n + j), a.box[k]);
@@ -254,11 +282,12 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
 #endif
     }
 #if DP_FF
+    // double-float -> float64 by moving bits (one float64 add per value)
     if (ACC == DP_ACC_FORCE) {
 #pragma unroll
-        for (int k = 0; k < D; ++k) f[k] = (double)acc_v[k] + facc[k].to_double();
+        for (int k = 0; k < D; ++k) f[k] = used64 ? (double)acc_v[k] + dpff_to_double(facc[k]) : dpff_to_double(facc[k]);
     }
-    return acc_s + sacc.to_double();
+    return used64 ? acc_s + dpff_to_double(sacc) : dpff_to_double(sacc);
 #else
     if (ACC == DP_ACC_FORCE) {
 #pragma unroll
@@ -278,7 +307,7 @@ extern "C" __global__ void __launch_bounds__(256) dp_forces(dp_pair_args a) {
 #pragma unroll
     for (int k = 0; k < DP_DIM; ++k) {
         a.out[k * a.n + i] = f[k];
-        finite = finite && isfinite(f[k]);
+        finite = finite && dp_isfinite_bits(f[k]);
     }
     if (!finite) atomicExch(&a.status->nonfinite, 1);
 }

@@ -69,7 +69,11 @@ class PairSurrogate:
     """The trained network for the costly terms of one pair potential."""
 
     def __init__(self, pair_potential_str: str, r_cut: float, r_min: float = 0.8, n_samples: int = 2 ** 20,
-                 seed: int = 0):
+                 seed: int = 0, sampling: str = "uniform"):
+        """Training samples r in [r_min, r_cut]: ``sampling`` "uniform" in r, or
+        "pairs" with density proportional to r^(D-1) for D = 3 (uniform in r^3,
+        as the pair distances of a homogeneous fluid), which weights the loss
+        as the pair sums (energy, virial) weigh the errors."""
         self.pair_potential_str = pair_potential_str
         self.r_cut = float(r_cut)
         self.r_min = float(r_min)
@@ -77,7 +81,13 @@ class PairSurrogate:
         if self.costly_str in ("0", ""):
             raise ValueError("the potential has no costly terms to learn")
         rng = np.random.default_rng(seed)
-        r = rng.uniform(self.r_min, self.r_cut, size=n_samples)
+        if sampling == "uniform":
+            r = rng.uniform(self.r_min, self.r_cut, size=n_samples)
+        elif sampling == "pairs":
+            r = np.cbrt(rng.uniform(self.r_min ** 3, self.r_cut ** 3, size=n_samples))
+        else:
+            raise ValueError(f"unknown sampling {sampling!r}")
+        self.sampling = sampling
         u, f = _eval_codegen_fp64(self.costly_str, self.r_cut, r)
         s = r * r
         f_times_r = f * r
@@ -111,7 +121,7 @@ class PairSurrogate:
         return out
 
     # --------------------------------------------------------------- training
-    def train(self, steps: int = 30000, batch: int = 16384, lr0: float = 2e-3, lr1: float = 1e-6, wf: float = 1.0,
+    def train(self, steps: int = 100000, batch: int = 16384, lr0: float = 2e-3, lr1: float = 1e-6, wf: float = 1.0,
               accurate: bool = False) -> np.ndarray:
         """Adam on the GPU; returns the minibatch loss of every step."""
         losses = np.empty(steps, dtype=np.float32)

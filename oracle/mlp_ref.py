@@ -2,8 +2,9 @@
 
 Forward, loss and gradients of the 1 -> 64 -> 64 -> 2 tanh network that the GPU
 trains (parameter layout as ``dompap_gb300.mlp``): w1[64], b1[64], W2[64][64]
-(row = output unit), b2[64], W3[2][64], b3[2]. The forward uses the same
-bf16-rounded weights as the GPU (``round_bf16``); loss per sample is
+(row = output unit), b2[64], W3[2][64], b3[2]. The forward rounds W2 to
+bf16 as the GPU does (``round_bf16``; w1 and W3 too when ``scalar_bf16``,
+the library's DP_MLP_SCALAR_BF16 build); loss per sample is
 ``(y0 - t0)^2 + wf (y1 - t1)^2``, averaged over the batch. Used to check the
 GPU gradients.
 """
@@ -34,10 +35,11 @@ def unpack(p: np.ndarray):
     return w1, b1, w2, b2, w3, b3
 
 
-def forward(p, x):
+def forward(p, x, scalar_bf16=False):
     """x: normalised inputs (B,). Returns y (B, 2) and the activations."""
     w1, b1, w2, b2, w3, b3 = unpack(p)
-    w1q, w2q, w3q = round_bf16(w1), round_bf16(w2), round_bf16(w3)
+    w2q = round_bf16(w2)
+    w1q, w3q = (round_bf16(w1), round_bf16(w3)) if scalar_bf16 else (w1, w3)
     h1 = np.tanh(np.outer(x, w1q) + b1)
     z2 = h1 @ w2q.T + b2
     h2 = np.tanh(z2)
@@ -45,9 +47,9 @@ def forward(p, x):
     return y, (h1, z2, h2, w2q, w3q)
 
 
-def loss_and_grad(p, x, t, wf=1.0):
+def loss_and_grad(p, x, t, wf=1.0, scalar_bf16=False):
     """Mean loss and its gradient with respect to the fp32 masters (straight-through bf16 rounding)."""
-    y, (h1, z2, h2, w2q, w3q) = forward(p, x)
+    y, (h1, z2, h2, w2q, w3q) = forward(p, x, scalar_bf16)
     b = x.shape[0]
     e = y - t
     loss = float(np.mean(e[:, 0] ** 2 + wf * e[:, 1] ** 2))
