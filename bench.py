@@ -604,7 +604,7 @@ def main():
     mean_k = float(np.mean(np.sum(np.asarray(sim.neighbor_list) != -1, axis=1))) if n <= 4_000_000 else 12.0
     dim = sim.get_dimensions_of_space()
     alg = {
-        "forces": 4 * mean_k + 16 * dim + 4,  # SURVEY per-particle bytes: list + count + own x + F write
+        "forces": 4 * mean_k + 16 * dim + 4,  # per particle: list + count + own x + F write
         "gjf_integrate": 72 * dim + 8,        # read x, v, beta, F, x_ref, mass, image; write x, v, beta, image
     }
     dominant = max(alg, key=lambda k: kt[k])
@@ -627,7 +627,11 @@ def main():
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
                      "algorithmic_bytes_per_particle": alg[dominant]},
         "kernel_ms": kt, "mean_neighbors": mean_k, "rebuilds_in_timed_region": rebuilds,
+        "conditional_rebuild_nodes": bool(st1.conditional_graphs),
     }
+    if dominant == "forces":
+        line["roofline"]["note"] = ("float64-parity pair arithmetic runs in double-float on the FP32 pipes: "
+                                    "the kernel is instruction-issue bound, far below the HBM roof")
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.workload, args.seed, steps_per_rebuild)
     if rank == 0 and not args.no_variants:

@@ -69,6 +69,8 @@ class DpStats(ctypes.Structure):
         ("cell_capacity", ctypes.c_int32),
         ("method_used", ctypes.c_int32),
         ("nl_cutoff", ctypes.c_double),
+        ("conditional_graphs", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
     ]
 
 

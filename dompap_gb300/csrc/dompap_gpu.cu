@@ -420,6 +420,12 @@ __global__ void k_rebuild_done(dp_dev_status* st) {
 
 __global__ void k_set_rebuild(dp_dev_status* st) { st->need_rebuild = 1; }
 
+// Condition of the graph's rebuild node: the sequence runs only when some
+// particle moved more than skin/2 (or a rebuild was requested).
+__global__ void k_rebuild_cond(const dp_dev_status* st, cudaGraphConditionalHandle h) {
+    cudaGraphSetConditional(h, st->need_rebuild ? 1u : 0u);
+}
+
 __global__ void k_advance_step(dp_dev_status* st, long long steps) { st->step += steps; }
 
 // Rows of the column-major list -> row-major (N, kout), each row sorted
@@ -545,17 +551,29 @@ __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
         uint32_t u[D];
         unsigned long long X[D];
         double xs[D];
+        // every load is issued before the first store (the arrays are not
+        // declared non-aliasing, so a store would otherwise order the loads
+        // of the next axis behind it)
+        double vin[D], xin[D], fin[D], bin[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) {
             const long long o = k * n + i;
-            double v = a.vel[o];
-            double x = a.pos[o];
-            const double F = a.force[o];
+            vin[k] = a.vel[o];
+            xin[k] = a.pos[o];
+            fin[k] = a.force[o];
+            bin[k] = NVE ? 0.0 : a.beta[o];
+        }
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            const long long o = k * n + i;
+            double v = vin[k];
+            double x = xin[k];
+            const double F = fin[k];
             if (NVE) {
                 v = v + c[4] * F;  // make_one_step_leap_frog (dompap/integrator.py:12)
             } else {
                 const double bn = c[3] * dp_f2d(z[k]);
-                v = c[0] * v + c[1] * F + c[2] * (a.beta[o] + bn);
+                v = c[0] * v + c[1] * F + c[2] * (bin[k] + bn);
                 a.beta[o] = bn;
             }
             x = x + v * a.dt;
@@ -864,7 +882,8 @@ struct GraphEntry {
     int kind;
     unsigned long long version;
     cudaGraphExec_t exec;
-    long long launches;
+    long long launches;          // launched every time the graph runs
+    long long rebuild_launches;  // launched per executed rebuild node (0: gated kernels, counted above)
 };
 
 struct dp_sim {
@@ -872,6 +891,8 @@ struct dp_sim {
     long long n = 0;
     int precision = DP_PREC_FP64;
     cudaStream_t stream = nullptr;
+    cudaStream_t cstream = nullptr;  // captures the bodies of conditional graph nodes
+    bool conditional_graphs = true;  // cleared if the driver rejects conditional nodes
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
     double *pos = nullptr, *vel = nullptr, *beta = nullptr, *force = nullptr, *pos_ref = nullptr;
@@ -1422,15 +1443,93 @@ static int update_nl(dp_sim* s, bool check, int* rebuilt) {
 }
 
 // --------------------------- graphs ---------------------------------------
-static int record_steps(dp_sim* s, long long steps, int kind, long long* launches) {
+// The rebuild sequence as an IF node of the graph being captured on
+// s->stream: a one-thread kernel sets the condition from need_rebuild, and the
+// body (captured on s->cstream) runs the cell and list kernels, so steps
+// without a rebuild launch none of them.
+static int capture_conditional_rebuild(dp_sim* s, cudaGraph_t graph, long long* launches,
+                                       long long* body_launches) {
+    // a handle belongs to one conditional node: one per step
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphConditionalHandleCreate(&h, graph, 0, 0));
+    k_rebuild_cond<<<1, 1, 0, s->stream>>>(s->dstat, h);
+    CK(cudaGetLastError());
+    *launches += 1;
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(s->stream, &cs, nullptr, nullptr, &deps, nullptr, &nd));
+    cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, graph, deps, nullptr, nd, &p));
+    CK(cudaStreamUpdateCaptureDependencies(s->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    CK(cudaStreamBeginCaptureToGraph(s->cstream, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                     cudaStreamCaptureModeThreadLocal));
+    std::swap(s->stream, s->cstream);
+    long long body = 0;
+    const int rc = launch_rebuild(s, &body);
+    std::swap(s->stream, s->cstream);
+    cudaGraph_t out = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s->cstream, &out);
+    RET(rc);
+    if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("conditional body capture: ") + cudaGetErrorString(e));
+    *body_launches = body;
+    return DP_OK;
+}
+
+// One chunk of steps into the graph being captured on s->stream; with
+// `conditional` the rebuild sequence goes into IF nodes, otherwise the gated
+// kernels are launched every step.
+static int record_steps(dp_sim* s, long long steps, int kind, cudaGraph_t graph, bool conditional,
+                        long long* launches, long long* rebuild_launches) {
+    *rebuild_launches = 0;
     for (long long t = 0; t < steps; ++t) {
-        RET(launch_rebuild(s, launches));
+        if (conditional)
+            RET(capture_conditional_rebuild(s, graph, launches, rebuild_launches));
+        else
+            RET(launch_rebuild(s, launches));
         RET(launch_pair(s, s->lib.forces, s->force, launches));
         RET(launch_integrate(s, kind, t, launches));
     }
     k_advance_step<<<1, 1, 0, s->stream>>>(s->dstat, steps);
     CK(cudaGetLastError());
     *launches += 1;
+    return DP_OK;
+}
+
+// Capture a chunk graph (conditional rebuild nodes when the driver takes
+// them) and instantiate it.
+static int build_graph(dp_sim* s, long long steps, int kind, bool conditional, GraphEntry* g) {
+    cudaGraph_t graph = nullptr;
+    CK(cudaGraphCreate(&graph, 0));
+    cudaError_t e = cudaStreamBeginCaptureToGraph(s->stream, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return fail(DP_ERR_CUDA, std::string("cudaStreamBeginCaptureToGraph: ") + cudaGetErrorString(e));
+    }
+    long long launches = 0, rebuild_launches = 0;
+    const int rc = record_steps(s, steps, kind, graph, conditional, &launches, &rebuild_launches);
+    cudaGraph_t captured = nullptr;
+    e = cudaStreamEndCapture(s->stream, &captured);
+    if (rc != DP_OK || e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return rc != DP_OK ? rc : fail(DP_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    }
+    g->steps = steps;
+    g->kind = kind;
+    g->version = s->version;
+    g->launches = launches;
+    g->rebuild_launches = rebuild_launches;
+    e = cudaGraphInstantiate(&g->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(DP_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    }
     return DP_OK;
 }
 
@@ -1450,21 +1549,14 @@ static int get_graph(dp_sim* s, long long steps, int kind, GraphEntry** out) {
             ++it;
         }
     }
-    cudaGraph_t graph;
-    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-    long long launches = 0;
-    const int rc = record_steps(s, steps, kind, &launches);
-    cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
-    if (rc != DP_OK) return rc;
-    if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
     GraphEntry g;
-    g.steps = steps;
-    g.kind = kind;
-    g.version = s->version;
-    g.launches = launches;
-    e = cudaGraphInstantiate(&g.exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    int rc = DP_ERR_CUDA;
+    if (s->conditional_graphs && s->cstream) {
+        rc = build_graph(s, steps, kind, true, &g);
+        // a driver without conditional nodes: the gated kernels from now on
+        if (rc != DP_OK) s->conditional_graphs = false;
+    }
+    if (rc != DP_OK) RET(build_graph(s, steps, kind, false, &g));
     s->graphs.push_back(g);
     *out = &s->graphs.back();
     return DP_OK;
@@ -1511,6 +1603,7 @@ static int run_impl(dp_sim* s, long long steps, int kind, float* ms) {
     while (done < steps) {
         const long long c = std::min(chunk, steps - done);
         const long long step0 = s->hstat->step;  // hstat is current: every path here ends in read_status
+        const long long rebuilds0 = s->hstat->rebuilds;
         RET(backup_state(s));
         GraphEntry* g = nullptr;
         RET(get_graph(s, c, kind, &g));
@@ -1531,7 +1624,7 @@ static int run_impl(dp_sim* s, long long steps, int kind, float* ms) {
             RET(write_status(s));
             continue;  // replay the chunk with the larger capacity
         }
-        s->launches_last += g->launches;
+        s->launches_last += g->launches + (s->hstat->rebuilds - rebuilds0) * g->rebuild_launches;
         done += c;
     }
     if (ms) {
@@ -1567,6 +1660,7 @@ int dp_create(int dim, int64_t n, int precision, dp_sim** out) {
         return rc;
     };
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->cstream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess) {
         rc = fail(DP_ERR_CUDA, std::string("stream/event creation: ") + cudaGetErrorString(cudaGetLastError()));
         return cleanup();
@@ -1625,6 +1719,7 @@ int dp_destroy(dp_sim* s) {
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->stream) cudaStreamDestroy(s->stream);
+    if (s->cstream) cudaStreamDestroy(s->cstream);
     delete s;
     return DP_OK;
 }
@@ -2075,6 +2170,7 @@ int dp_get_stats(dp_sim* s, dp_stats* st) {
     st->cell_capacity = s->ccap;
     st->method_used = s->use_cells ? DP_NL_CELL : DP_NL_ALLPAIRS;
     st->nl_cutoff = s->cutoff;
+    st->conditional_graphs = s->conditional_graphs ? 1 : 0;
     return DP_OK;
 }
 

@@ -203,16 +203,17 @@ __device__ __forceinline__ float dp_i2f(int n) {
     return fmaf(dp_small_int(n >> 16), 65536.0f, dp_small_int(n & 0xFFFF));
 }
 
-// float -> double by moving the bits (sign, exponent rebiased, mantissa);
-// subnormals, infinities and NaN take the conversion instruction.
+// float -> double by moving the bits (sign, exponent rebiased, mantissa),
+// without branches: infinities and NaN keep their class, float subnormals
+// become signed zeros (below 1.2e-38; no value that reaches this function
+// needs them).
 __device__ __forceinline__ double dp_f2d(float z) {
     const uint32_t b = __float_as_uint(z);
     const uint32_t e = (b >> 23) & 0xFFu;
-    if ((b & 0x7FFFFFFFu) == 0u) return __longlong_as_double((long long)((unsigned long long)b << 32));
-    if (e == 0u || e == 0xFFu) return (double)z;
-    return __longlong_as_double((long long)(((unsigned long long)(b >> 31) << 63) |
-                                            ((unsigned long long)(e + (1023u - 127u)) << 52) |
-                                            ((unsigned long long)(b & 0x7FFFFFu) << 29)));
+    const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+    const unsigned long long ed = e == 0u ? 0ull : (e == 0xFFu ? 0x7FFull : (unsigned long long)(e + (1023u - 127u)));
+    const unsigned long long mant = e == 0u ? 0ull : (unsigned long long)(b & 0x7FFFFFu) << 29;
+    return __longlong_as_double((long long)(sign | (ed << 52) | mant));
 }
 
 template <int D>

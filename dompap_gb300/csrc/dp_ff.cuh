@@ -73,14 +73,26 @@ __device__ __forceinline__ bool operator>(dpff x, dpff y) { return y < x; }
 __device__ __forceinline__ bool operator<=(dpff x, dpff y) { return !(y < x); }
 __device__ __forceinline__ bool operator>=(dpff x, dpff y) { return !(x < y); }
 
-// 1/sqrt(q): float seed refined by one Newton step in double-float.
+// 1/sqrt(q): the float estimate y (rsqrtf, then one float Newton step, so
+// y is within about an ulp and e below is ~2^-24) refined by one Newton step
+// with its second-order term, y (1 + e/2 + 3e^2/8), e = 1 - q y^2. y^2 and
+// q.hi y^2 are split exactly by FMA and 1 - p is exact (p is within a few
+// ulp of 1); the result is good to ~1.2e-14 relative.
 __device__ __forceinline__ dpff dpff_rsqrt(dpff q) {
     const float y0 = rsqrtf(q.hi);
-    // e = 1 - q y0^2
-    const dpff qy = dpff_mul_f(q, y0);
-    const dpff qyy = dpff_mul_f(qy, y0);
-    const dpff e = dpff(1.0f, 0.0f) - qyy;
-    return dpff(y0, 0.0f) + dpff_mul_f(e, 0.5f * y0);
+    const float y = fmaf(0.5f * y0, fmaf(-(q.hi * y0), y0, 1.0f), y0);
+    const float t = y * y;
+    const float tl = fmaf(y, y, -t);   // y^2 = t + tl
+    const float p = q.hi * t;
+    const float pl = fmaf(q.hi, t, -p);  // q.hi t = p + pl
+    const float e = ((1.0f - p) - pl) - fmaf(q.hi, tl, q.lo * t);
+    return dpff_quick_two_sum(y, y * e * fmaf(0.375f, e, 0.5f));
+}
+
+// x^2 unnormalised: (p, e) with p + e = x^2 to ~2^-48 (for dpff_accumulate).
+__device__ __forceinline__ dpff dpff_sqr_unnormalised(dpff x) {
+    const float p = x.hi * x.hi;
+    return dpff(p, fmaf(x.hi + x.hi, x.lo, fmaf(x.hi, x.hi, -p)));
 }
 
 __device__ __forceinline__ dpff dpff_add_f(dpff x, float b) {
@@ -90,15 +102,18 @@ __device__ __forceinline__ dpff dpff_add_f(dpff x, float b) {
 
 // int64 -> double-float (rounded to ~48 bits) without 64-bit conversion
 // instructions: v = a 2^42 + b 2^20 + c with a in [-2^21, 2^21), b < 2^22,
-// c < 2^20, each piece an exact float; a 2^42 + b 2^20 has at most 44
-// significant bits, so its TwoSum is exact, and c is added last.
+// c < 2^20, each piece an exact float. fa + fb is a multiple of 2^20 and
+// |fa| >= 2^42 > |fb| unless fa = 0, so Fast2Sum (QuickTwoSum) is exact for
+// it and again for adding fc (|fc| < 2^20 <= |fa + fb| unless that is 0).
 __device__ __forceinline__ dpff dpff_from_ll(long long v) {
     const int a = (int)(v >> 42);
     const int b = (int)(((unsigned long long)v >> 20) & 0x3FFFFFull);
     const int c = (int)((unsigned long long)v & 0xFFFFFull);
     const float fa = dp_small_int(a) * 4398046511104.0f;  // 2^42
     const float fb = dp_small_int(b) * 1048576.0f;        // 2^20
-    return dpff_add_f(dpff_two_sum(fa, fb), dp_small_int(c));
+    const dpff ab = dpff_quick_two_sum(fa, fb);
+    const dpff t = dpff_quick_two_sum(ab.hi, dp_small_int(c));
+    return dpff_quick_two_sum(t.hi, t.lo + ab.lo);
 }
 
 // Compensated accumulation s += v (cascaded summation in the manner of
@@ -109,6 +124,16 @@ __device__ __forceinline__ void dpff_accumulate(dpff& s, dpff v) {
     const dpff t = dpff_two_sum(s.hi, v.hi);
     s.hi = t.hi;
     s.lo += t.lo + v.lo;
+}
+
+// s += x y without normalising the product first: its leading float p and
+// the FMA-exact rounding error plus cross terms go to the two parts of s.
+__device__ __forceinline__ void dpff_accumulate_prod(dpff& s, dpff x, dpff y) {
+    const float p = x.hi * y.hi;
+    const float pe = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, fmaf(x.hi, y.hi, -p)));
+    const dpff t = dpff_two_sum(s.hi, p);
+    s.hi = t.hi;
+    s.lo += t.lo + pe;
 }
 
 // hi + lo in float64 with the two widenings done on bit patterns.

@@ -185,9 +185,10 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
             dpff d[D];
 #pragma unroll
             for (int k = 0; k < D; ++k) d[k] = dpff_from_ll((long long)(Xi[k] - Xj[k])) * U[k];
-            dpff q = d[0] * d[0];
+            dpff q = dpff_sqr_unnormalised(d[0]);
 #pragma unroll
-            for (int k = 1; k < D; ++k) q = q + d[k] * d[k];
+            for (int k = 1; k < D; ++k) dpff_accumulate(q, dpff_sqr_unnormalised(d[k]));
+            q = dpff_quick_two_sum(q.hi, q.lo);
             const dpff rinv = dpff_rsqrt(q);
             const dpff r = q * rinv;
 #if DP_PMODE == 0
@@ -216,7 +217,7 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
                     const dpff g = feps * dp_pair_f<dpff>(s, sinv) * rinv;
 #endif
 #pragma unroll
-                    for (int k = 0; k < D; ++k) dpff_accumulate(facc[k], g * d[k]);
+                    for (int k = 0; k < D; ++k) dpff_accumulate_prod(facc[k], g, d[k]);
                 } else if (ACC == DP_ACC_ENERGY) {
                     dpff_accumulate(sacc, feps * dp_pair_u<dpff>(s, sinv));
                 } else if (ACC == DP_ACC_VIRIAL) {
@@ -297,8 +298,14 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
 #endif
 }
 
-// F (SoA float64) for every particle. One thread per particle.
-extern "C" __global__ void __launch_bounds__(256) dp_forces(dp_pair_args a) {
+// F (SoA float64) for every particle. One thread per particle; the
+// double-float loop is limited to 64 registers (four 256-thread CTAs per SM).
+#if DP_FF
+#define DP_FORCES_BOUNDS __launch_bounds__(256, 4)
+#else
+#define DP_FORCES_BOUNDS __launch_bounds__(256)
+#endif
+extern "C" __global__ void DP_FORCES_BOUNDS dp_forces(dp_pair_args a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     double f[DP_DIM];

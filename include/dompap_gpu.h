@@ -57,6 +57,10 @@ typedef struct dp_stats {
     int32_t cell_capacity;      /* particles per cell slot array                      */
     int32_t method_used;        /* DP_NL_CELL or DP_NL_ALLPAIRS                       */
     double nl_cutoff;           /* largest sigma * r_cut + skin                       */
+    int32_t conditional_graphs; /* 1: run() skips the rebuild kernels on steps that need
+                                   no rebuild (conditional graph nodes); 0: they are
+                                   launched every step and return at once            */
+    int32_t pad;
 } dp_stats;
 
 /* Last error message of the calling thread ("" if none). */
