@@ -42,7 +42,7 @@ def write_embedded() -> str:
     parts = []
     for name, sym in (("dp_common.cuh", "dp_src_common"), ("pair_kernels.cuh", "dp_src_pair"),
                       ("batch_kernels.cuh", "dp_src_batch"), ("mlp_common.cuh", "dp_src_mlp"),
-                      ("dp_ff.cuh", "dp_src_ff")):
+                      ("dp_ff.cuh", "dp_src_ff"), ("dp_integrate.cuh", "dp_src_integrate")):
         with open(os.path.join(CSRC, name)) as fh:
             text = fh.read()
         if ')DPSRC"' in text:
@@ -102,13 +102,15 @@ def check_pair_kernels(verbose: bool = True) -> None:
         batch = fh.read()
     with open(os.path.join(CSRC, "dp_ff.cuh")) as fh:
         ffsrc = fh.read()
+    with open(os.path.join(CSRC, "dp_integrate.cuh")) as fh:
+        integ = fh.read()
     for dim in (2, 3, 4):
         for real, is_float in (("double", 0), ("float", 1)):
             for pmode in (0, 1, 2):
                 src = (f"#define DP_DIM {dim}\n#define DP_REAL {real}\n#define DP_REAL_IS_FLOAT {is_float}\n"
                        f"#define DP_PMODE {pmode}\n#define DP_SIGMA_ONE {int(pmode == 0)}\n"
                        f"#define DP_EPS_ONE {int(pmode == 0)}\n#define DP_FF {1 - is_float}\n#include <cstdint>\n"
-                       + common + (ffsrc if not is_float else "") + SAMPLE_POTENTIAL + pair
+                       + common + integ + (ffsrc if not is_float else "") + SAMPLE_POTENTIAL + pair
                        + (batch if is_float and pmode == 0 else ""))
                 path = os.path.join(BUILD, f"pair_check_{dim}_{real}_{pmode}.cu")
                 with open(path, "w") as fh:

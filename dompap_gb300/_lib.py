@@ -39,6 +39,7 @@ DP_KERNEL_GJF = 1
 DP_KERNEL_NVE = 2
 DP_KERNEL_REBUILD = 3
 DP_KERNEL_SKIN = 4
+DP_KERNEL_STEP = 5
 
 _ERROR_NAMES = {
     DP_ERR_ARG: "invalid argument",

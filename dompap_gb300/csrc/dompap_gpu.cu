@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <string>
@@ -32,6 +33,7 @@
 
 #include "dompap_gpu.h"
 #include "dp_common.cuh"
+#include "dp_integrate.cuh"
 #include "dp_embedded.h"
 #include "mlp_common.cuh"
 #include "mlp_train.cuh"  // dp_src_common[], dp_src_pair[] (generated at build time)
@@ -161,21 +163,6 @@ struct SkinArgs {
 };
 
 template <int D>
-__device__ __forceinline__ bool skin_old(const SkinArgs& a, long long i, const uint32_t* u, const double* x) {
-    typedef typename dp_shadow_t<D>::type sh_t;
-    uint32_t uref[D];
-    dp_shadow_unpack<D>(((const sh_t*)a.shadow_ref)[i], uref);
-    float df[D];
-    const float qf = dp_shadow_q<D>(u, uref, a.unit, df);
-    if (qf <= a.thr_lo) return false;
-    if (qf > a.thr_hi) return true;
-    double d[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) d[k] = dp_min_image(x[k] - a.pos_ref[k * a.n + i], a.box[k]);
-    return dp_sqsum_exact<D>(d) > a.thr;
-}
-
-template <int D>
 __global__ void k_skin_check(SkinArgs a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     bool old = false;
@@ -186,7 +173,7 @@ __global__ void k_skin_check(SkinArgs a) {
         double x[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) x[k] = a.pos[k * a.n + i];
-        old = skin_old<D>(a, i, u, x);
+        old = dp_skin_old<D>(a.shadow_ref, a.pos_ref, a.n, a.unit, a.box, a.thr, a.thr_lo, a.thr_hi, i, u, x);
     }
     if (__any_sync(0xffffffffu, old) && (threadIdx.x & 31) == 0) atomicExch(&a.st->need_rebuild, 1);
 }
@@ -422,11 +409,19 @@ __global__ void k_set_rebuild(dp_dev_status* st) { st->need_rebuild = 1; }
 
 // Condition of the graph's rebuild node: the sequence runs only when some
 // particle moved more than skin/2 (or a rebuild was requested).
-__global__ void k_rebuild_cond(const dp_dev_status* st, cudaGraphConditionalHandle h) {
+// reset_far: the previous (fused) step wrapped every position.
+__global__ void k_rebuild_cond(dp_dev_status* st, cudaGraphConditionalHandle h, int reset_far) {
+    if (reset_far) st->far = 0;
     cudaGraphSetConditional(h, st->need_rebuild ? 1u : 0u);
 }
 
-__global__ void k_advance_step(dp_dev_status* st, long long steps) { st->step += steps; }
+__global__ void k_clear_far(dp_dev_status* st) { st->far = 0; }
+
+// End of a graph of steps; clear_far: its last (fused) step wrapped every position.
+__global__ void k_advance_step(dp_dev_status* st, long long steps, int clear_far) {
+    st->step += steps;
+    if (clear_far) st->far = 0;
+}
 
 // Rows of the column-major list -> row-major (N, kout), each row sorted
 // ascending and -1 padded (dompap's neighbor_list layout).
@@ -461,167 +456,20 @@ __global__ void k_nl_export(const int32_t* __restrict__ nl, const int32_t* __res
 // Mass handling: MASSMODE 0 one mass for all particles (coefficients as
 // arguments), 1 per-particle class index into a coefficient table, 2
 // per-particle masses (coefficients computed in the kernel).
-struct IntArgs {
-    double* pos;
-    double* vel;
-    double* beta;
-    const double* force;
-    int32_t* img;
-    void* shadow;
-    void* pos64;
-    const double* pos_ref;
-    const void* shadow_ref;
-    const uint8_t* mclass;
-    const double* mcoef;  // [class][5]: a, b*dt/m, b/(2m), sqrt(2 alpha T dt), dt/m
-    const double* mass;   // MASSMODE 2
-    dp_dev_status* st;
-    long long n;
-    double box[DP_MAX_DIM];
-    double scale[DP_MAX_DIM];
-    double scale64[DP_MAX_DIM];
-    float unit[DP_MAX_DIM];
-    double thr;  // (skin/2)^2
-    float thr_lo, thr_hi;
-    double dt;
-    double coef[5];  // MASSMODE 0
-    double temperature;
-    double tau;
-    unsigned long long seed;
-    long long step_offset;
-};
-
-__device__ __forceinline__ void gjf_coefficients(double m, double dt, double T, double tau, double* c) {
-    // dompap/integrator.py:29-36
-    const double alpha = m / tau;
-    const double beta_variance = 2 * alpha * T * dt;
-    const double numerator = 1.0 - alpha * dt / 2.0 / m;
-    const double denominator = 1.0 + alpha * dt / 2.0 / m;
-    const double a = numerator / denominator;
-    const double b = 1 / denominator;
-    c[0] = a;
-    c[1] = b * dt / m;
-    c[2] = b / 2 / m;
-    c[3] = sqrt(beta_variance);
-    c[4] = dt / m;
-}
-
-template <int D, int MASSMODE>
-__device__ __forceinline__ void load_coef(const IntArgs& a, long long i, double* c) {
-    if (MASSMODE == 0) {
-#pragma unroll
-        for (int t = 0; t < 5; ++t) c[t] = a.coef[t];
-    } else if (MASSMODE == 1) {
-        const int cl = a.mclass[i];
-#pragma unroll
-        for (int t = 0; t < 5; ++t) c[t] = __ldg(a.mcoef + cl * 5 + t);
-    } else {
-        gjf_coefficients(a.mass[i], a.dt, a.temperature, a.tau, c);
-    }
-}
-
-// Wrap into [0, L) exactly as wrap_into_box (dompap/positions.py:90-98):
-// shift = floor(x / L), image += shift, x -= shift * L. For 0 <= x < L the
-// rounded x / L is < 1, so the shift is 0 and the division is skipped.
-__device__ __forceinline__ double wrap_axis(double x, double L, int32_t& image) {
-    if (!(x >= 0.0 && x < L)) {
-        const double s = floor(x / L);
-        image += (int32_t)s;
-        x -= s * L;
-    }
-    return x;
-}
-
-// Langevin G-JF leap-frog (dompap/integrator.py:17-40, arXiv:1303.7011
-// Sec. II.C eqs. 16-17) or NVE leap-frog (:5-14), then the wrap into the box,
-// the fixed-point shadow and the skin test for the next step. The float64
-// position is converted to fixed point once; a value outside [0, 2^32) is the
-// only case that needs the wrap (done exactly as wrap_into_box), and the skin
-// test reads the shadows (float64 only near the threshold).
+// The per-particle step is dp_integrate_one (dp_integrate.cuh). This kernel
+// integrates in place after a separate force kernel (the surrogate mode, and
+// the timing of the integrator alone); the other modes fuse it into the pair
+// kernel.
 template <int D, int MASSMODE, bool NVE, bool WRITE64>
-__global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
+__global__ void __launch_bounds__(kBlock) k_integrate(dp_int_args a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st->far = 0;  // every position is wrapped below
     bool old = false, bad = false;
     if (i < a.n) {
-        const long long n = a.n;
-        double c[5];
-        load_coef<D, MASSMODE>(a, i, c);
-        float z[4];
-        if (!NVE) dp_normals4(a.seed, (unsigned long long)(a.st->step + a.step_offset), (uint32_t)i, z);
-        uint32_t u[D];
-        unsigned long long X[D];
-        double xs[D];
-        // every load is issued before the first store (the arrays are not
-        // declared non-aliasing, so a store would otherwise order the loads
-        // of the next axis behind it)
-        double vin[D], xin[D], fin[D], bin[D];
+        double F[D];
 #pragma unroll
-        for (int k = 0; k < D; ++k) {
-            const long long o = k * n + i;
-            vin[k] = a.vel[o];
-            xin[k] = a.pos[o];
-            fin[k] = a.force[o];
-            bin[k] = NVE ? 0.0 : a.beta[o];
-        }
-#pragma unroll
-        for (int k = 0; k < D; ++k) {
-            const long long o = k * n + i;
-            double v = vin[k];
-            double x = xin[k];
-            const double F = fin[k];
-            if (NVE) {
-                v = v + c[4] * F;  // make_one_step_leap_frog (dompap/integrator.py:12)
-            } else {
-                const double bn = c[3] * dp_f2d(z[k]);
-                v = c[0] * v + c[1] * F + c[2] * (bin[k] + bn);
-                a.beta[o] = bn;
-            }
-            x = x + v * a.dt;
-            if (WRITE64) {
-                // one product gives the wrap test (its bit pattern, an integer
-                // compare), the 64-bit fixed point and the 32-bit shadow
-                double p = x * a.scale64[k];
-                const long long pb = __double_as_longlong(p);
-                if (!(pb >= 0 && pb < 0x43F0000000000000LL)) {  // p outside [0, 2^64)
-                    int32_t im = a.img[o];
-                    x = wrap_axis(x, a.box[k], im);
-                    a.img[o] = im;
-                    bad = bad || !isfinite(x);
-                    p = (x >= 0.0 && x < a.box[k]) ? x * a.scale64[k] : 0.0;
-                }
-                X[k] = dp_fixed64_of(p);
-                u[k] = (uint32_t)(X[k] >> 32);
-            } else {
-                const long long t = __double2ll_rd(x * a.scale[k]);
-                if (t < 0 || t >= 4294967296LL) {
-                    int32_t im = a.img[o];
-                    x = wrap_axis(x, a.box[k], im);
-                    a.img[o] = im;
-                    u[k] = dp_fixed(x, a.scale[k]);
-                    bad = bad || !isfinite(x);
-                } else {
-                    u[k] = (uint32_t)t;
-                }
-            }
-            a.vel[o] = v;
-            a.pos[o] = x;
-            xs[k] = x;
-        }
-        ((typename dp_shadow_t<D>::type*)a.shadow)[i] = dp_shadow_pack<D>(u);
-        if (WRITE64) ((typename dp_fixed64_t<D>::type*)a.pos64)[i] = dp_fixed64_pack<D>(X);
-        SkinArgs sa;
-        sa.pos_ref = a.pos_ref;
-        sa.shadow_ref = a.shadow_ref;
-        sa.n = n;
-        sa.thr = a.thr;
-        sa.thr_lo = a.thr_lo;
-        sa.thr_hi = a.thr_hi;
-#pragma unroll
-        for (int k = 0; k < D; ++k) {
-            sa.box[k] = a.box[k];
-            sa.unit[k] = a.unit[k];
-        }
-        old = skin_old<D>(sa, i, u, xs);
+        for (int k = 0; k < D; ++k) F[k] = a.force[k * a.n + i];
+        old = dp_integrate_one<D, MASSMODE, NVE, WRITE64>(a, i, F, bad);
     }
     const bool any_old = __any_sync(0xffffffffu, old);
     const bool any_bad = __any_sync(0xffffffffu, bad);
@@ -633,7 +481,7 @@ __global__ void __launch_bounds__(kBlock) k_integrate(IntArgs a) {
 
 // sum_n m_n |v_n|^2, per-block partials.
 template <int D, int MASSMODE>
-__global__ void __launch_bounds__(kBlock) k_sum_mv2(IntArgs a, const double* class_mass, double* partial) {
+__global__ void __launch_bounds__(kBlock) k_sum_mv2(dp_int_args a, const double* class_mass, double* partial) {
     __shared__ double smem[32];
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double v = 0.0;
@@ -675,7 +523,7 @@ __global__ void k_normals(unsigned long long seed, long long step, double* out, 
 
 // wrap_into_box on demand (dompap/positions.py:90-98), with the shadow update.
 template <int D>
-__global__ void k_wrap(IntArgs a) {
+__global__ void k_wrap(dp_int_args a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st->far = 0;
     if (i >= a.n) return;
@@ -686,14 +534,14 @@ __global__ void k_wrap(IntArgs a) {
         const long long o = k * a.n + i;
         int32_t im = a.img[o];
         const int32_t im0 = im;
-        const double x = wrap_axis(a.pos[o], a.box[k], im);
-        a.pos[o] = x;
+        const double x = dp_wrap_axis(a.pos[o], a.box[k], im);
+        a.pos_out[o] = x;
         if (im != im0) a.img[o] = im;
-        u[k] = dp_fixed(x, a.scale[k]);
         X[k] = fixed64_wrapped(x, a.box[k], a.scale64[k]);
+        u[k] = (uint32_t)(X[k] >> 32);
     }
-    ((typename dp_shadow_t<D>::type*)a.shadow)[i] = dp_shadow_pack<D>(u);
-    ((typename dp_fixed64_t<D>::type*)a.pos64)[i] = dp_fixed64_pack<D>(X);
+    ((typename dp_shadow_t<D>::type*)a.shadow_out)[i] = dp_shadow_pack<D>(u);
+    ((typename dp_fixed64_t<D>::type*)a.pos64_out)[i] = dp_fixed64_pack<D>(X);
 }
 
 // Pair-distance histogram for g(r) (dompap/positions.py:58-87): all ordered
@@ -818,6 +666,7 @@ static double* g_noalloc_addr[64] = {nullptr};
 struct PairLib {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t forces = nullptr, energy = nullptr, virial = nullptr, laplacian = nullptr, eval = nullptr;
+    cudaKernel_t step = nullptr;  // fused forces + integrate (not in the surrogate program)
     cudaKernel_t batch[4] = {nullptr, nullptr, nullptr, nullptr};  // 128, 256, 512, 1024 threads
     cudaKernel_t forces_mlp = nullptr, energy_mlp = nullptr, virial_mlp = nullptr;
 };
@@ -858,6 +707,7 @@ static int compile_pair_lib(const std::string& src, PairLib* out) {
     CK(cudaLibraryGetKernel(&pl.virial, pl.lib, "dp_virial"));
     CK(cudaLibraryGetKernel(&pl.laplacian, pl.lib, "dp_laplacian"));
     CK(cudaLibraryGetKernel(&pl.eval, pl.lib, "dp_eval_pair"));
+    if (src.find("#define DP_MLP 1") == std::string::npos) CK(cudaLibraryGetKernel(&pl.step, pl.lib, "dp_step"));
     if (src.find("#define DP_MLP 1") != std::string::npos) {
         CK(cudaLibraryGetKernel(&pl.forces_mlp, pl.lib, "dp_forces_mlp"));
         CK(cudaLibraryGetKernel(&pl.energy_mlp, pl.lib, "dp_energy_mlp"));
@@ -884,6 +734,8 @@ struct GraphEntry {
     cudaGraphExec_t exec;
     long long launches;          // launched every time the graph runs
     long long rebuild_launches;  // launched per executed rebuild node (0: gated kernels, counted above)
+    bool fused = false;          // dp_step graph: each step moves the positions to the other buffer set
+    const double* pos_key = nullptr;  // current position buffer when the graph was captured
 };
 
 struct dp_sim {
@@ -893,6 +745,12 @@ struct dp_sim {
     cudaStream_t stream = nullptr;
     cudaStream_t cstream = nullptr;  // captures the bodies of conditional graph nodes
     bool conditional_graphs = true;  // cleared if the driver rejects conditional nodes
+    bool fused_step = true;          // run() uses dp_step (DOMPAP_FUSED_STEP=0: separate kernels)
+    // second set of position buffers: a fused step reads pos/shadow/pos64 and
+    // writes these, then the two sets change roles
+    double* pos_alt = nullptr;
+    void* shadow_alt = nullptr;
+    void* pos64_alt = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
     double *pos = nullptr, *vel = nullptr, *beta = nullptr, *force = nullptr, *pos_ref = nullptr;
@@ -1266,15 +1124,17 @@ static int launch_pair(dp_sim* s, cudaKernel_t k, double* out, long long* launch
     return DP_OK;
 }
 
-static void fill_int_args(const dp_sim* s, IntArgs& a, long long step_offset) {
+// Integrator arguments; the outputs default to the current buffers (in place).
+static void fill_int_args(const dp_sim* s, dp_int_args& a, long long step_offset, int kind = DP_INT_GJF) {
     memset(&a, 0, sizeof(a));
     a.pos = s->pos;
+    a.pos_out = s->pos;
     a.vel = s->vel;
     a.beta = s->beta;
     a.force = s->force;
     a.img = s->img;
-    a.shadow = s->shadow;
-    a.pos64 = s->pos64;
+    a.shadow_out = s->shadow;
+    a.pos64_out = s->pos64;
     a.pos_ref = s->pos_ref;
     a.shadow_ref = s->shadow_ref;
     a.mclass = s->mclass;
@@ -1283,7 +1143,7 @@ static void fill_int_args(const dp_sim* s, IntArgs& a, long long step_offset) {
     a.st = s->dstat;
     a.n = s->n;
     for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
-    fill_scale(s, a.scale, a.unit);
+    fill_scale(s, nullptr, a.unit);
     for (int k = 0; k < DP_MAX_DIM; ++k) a.scale64[k] = 18446744073709551616.0 / ((k < s->dim) ? s->box[k] : 1.0);
     a.thr = (0.5 * s->skin) * (0.5 * s->skin);
     bracket(s, 0.5 * s->skin, &a.thr_lo, &a.thr_hi);
@@ -1306,10 +1166,12 @@ static void fill_int_args(const dp_sim* s, IntArgs& a, long long step_offset) {
     a.tau = s->tau;
     a.seed = s->seed;
     a.step_offset = step_offset;
+    a.massmode = s->mass_mode;
+    a.nve = kind == DP_INT_NVE ? 1 : 0;
 }
 
 template <int D, bool NVE, bool W64>
-static void launch_integrate_dw(dp_sim* s, const IntArgs& a) {
+static void launch_integrate_dw(dp_sim* s, const dp_int_args& a) {
     const unsigned g = grid_for(s->n, kBlock);
     switch (s->mass_mode) {
         case 0: k_integrate<D, 0, NVE, W64><<<g, kBlock, 0, s->stream>>>(a); break;
@@ -1320,7 +1182,7 @@ static void launch_integrate_dw(dp_sim* s, const IntArgs& a) {
 
 // The 64-bit fixed point is only read by the float64-parity pair kernels.
 template <int D, bool NVE>
-static void launch_integrate_d(dp_sim* s, const IntArgs& a) {
+static void launch_integrate_d(dp_sim* s, const dp_int_args& a) {
     if (s->precision == DP_PREC_FP64)
         launch_integrate_dw<D, NVE, true>(s, a);
     else
@@ -1328,8 +1190,8 @@ static void launch_integrate_d(dp_sim* s, const IntArgs& a) {
 }
 
 static int launch_integrate(dp_sim* s, int kind, long long step_offset, long long* launches) {
-    IntArgs a;
-    fill_int_args(s, a, step_offset);
+    dp_int_args a;
+    fill_int_args(s, a, step_offset, kind);
     const bool nve = kind == DP_INT_NVE;
     switch (s->dim) {
         case 2: nve ? launch_integrate_d<2, true>(s, a) : launch_integrate_d<2, false>(s, a); break;
@@ -1447,12 +1309,12 @@ static int update_nl(dp_sim* s, bool check, int* rebuilt) {
 // s->stream: a one-thread kernel sets the condition from need_rebuild, and the
 // body (captured on s->cstream) runs the cell and list kernels, so steps
 // without a rebuild launch none of them.
-static int capture_conditional_rebuild(dp_sim* s, cudaGraph_t graph, long long* launches,
+static int capture_conditional_rebuild(dp_sim* s, cudaGraph_t graph, bool reset_far, long long* launches,
                                        long long* body_launches) {
     // a handle belongs to one conditional node: one per step
     cudaGraphConditionalHandle h;
     CK(cudaGraphConditionalHandleCreate(&h, graph, 0, 0));
-    k_rebuild_cond<<<1, 1, 0, s->stream>>>(s->dstat, h);
+    k_rebuild_cond<<<1, 1, 0, s->stream>>>(s->dstat, h, reset_far ? 1 : 0);
     CK(cudaGetLastError());
     *launches += 1;
     cudaStreamCaptureStatus cs;
@@ -1480,21 +1342,63 @@ static int capture_conditional_rebuild(dp_sim* s, cudaGraph_t graph, long long* 
     return DP_OK;
 }
 
+static bool use_fused_step(const dp_sim* s) {
+    return s->fused_step && s->precision != DP_PREC_MLP && s->lib.step != nullptr;
+}
+
+// The two position buffer sets change roles (host pointers only).
+static void swap_position_buffers(dp_sim* s) {
+    std::swap(s->pos, s->pos_alt);
+    std::swap(s->shadow, s->shadow_alt);
+    std::swap(s->pos64, s->pos64_alt);
+}
+
+// Fused step: forces from the current buffers, integration into the others.
+static int launch_step(dp_sim* s, int kind, long long step_offset, long long* launches) {
+    dp_pair_args pa;
+    fill_pair_args(s, pa, nullptr);
+    dp_int_args ia;
+    fill_int_args(s, ia, step_offset, kind);
+    ia.force = nullptr;
+    ia.pos_out = s->pos_alt;
+    ia.shadow_out = s->shadow_alt;
+    ia.pos64_out = s->pos64_alt;
+    void* args[] = {&pa, &ia};
+    CK(cudaLaunchKernel((const void*)s->lib.step, dim3(grid_for(s->n, kBlock)), dim3(kBlock), args, 0, s->stream));
+    if (launches) *launches += 1;
+    return DP_OK;
+}
+
 // One chunk of steps into the graph being captured on s->stream; with
 // `conditional` the rebuild sequence goes into IF nodes, otherwise the gated
-// kernels are launched every step.
-static int record_steps(dp_sim* s, long long steps, int kind, cudaGraph_t graph, bool conditional,
+// kernels are launched every step. A fused chunk swaps the host's position
+// pointers once per captured step (the caller undoes that until the graph
+// has run).
+static int record_steps(dp_sim* s, long long steps, int kind, cudaGraph_t graph, bool conditional, bool fused,
                         long long* launches, long long* rebuild_launches) {
     *rebuild_launches = 0;
     for (long long t = 0; t < steps; ++t) {
-        if (conditional)
-            RET(capture_conditional_rebuild(s, graph, launches, rebuild_launches));
-        else
+        // after a fused step every position is wrapped: clear `far` before the
+        // list check and the pair loop read it
+        const bool reset_far = fused && t > 0;
+        if (conditional) {
+            RET(capture_conditional_rebuild(s, graph, reset_far, launches, rebuild_launches));
+        } else {
+            if (reset_far) {
+                k_clear_far<<<1, 1, 0, s->stream>>>(s->dstat);
+                *launches += 1;
+            }
             RET(launch_rebuild(s, launches));
-        RET(launch_pair(s, s->lib.forces, s->force, launches));
-        RET(launch_integrate(s, kind, t, launches));
+        }
+        if (fused) {
+            RET(launch_step(s, kind, t, launches));
+            swap_position_buffers(s);
+        } else {
+            RET(launch_pair(s, s->lib.forces, s->force, launches));
+            RET(launch_integrate(s, kind, t, launches));
+        }
     }
-    k_advance_step<<<1, 1, 0, s->stream>>>(s->dstat, steps);
+    k_advance_step<<<1, 1, 0, s->stream>>>(s->dstat, steps, fused && steps > 0 ? 1 : 0);
     CK(cudaGetLastError());
     *launches += 1;
     return DP_OK;
@@ -1511,7 +1415,11 @@ static int build_graph(dp_sim* s, long long steps, int kind, bool conditional, G
         return fail(DP_ERR_CUDA, std::string("cudaStreamBeginCaptureToGraph: ") + cudaGetErrorString(e));
     }
     long long launches = 0, rebuild_launches = 0;
-    const int rc = record_steps(s, steps, kind, graph, conditional, &launches, &rebuild_launches);
+    const bool fused = use_fused_step(s);
+    const double* pos_key = s->pos;
+    const int rc = record_steps(s, steps, kind, graph, conditional, fused, &launches, &rebuild_launches);
+    // the graph has not run yet: put the position pointers back
+    while (s->pos != pos_key) swap_position_buffers(s);
     cudaGraph_t captured = nullptr;
     e = cudaStreamEndCapture(s->stream, &captured);
     if (rc != DP_OK || e != cudaSuccess) {
@@ -1524,6 +1432,8 @@ static int build_graph(dp_sim* s, long long steps, int kind, bool conditional, G
     g->version = s->version;
     g->launches = launches;
     g->rebuild_launches = rebuild_launches;
+    g->fused = fused;
+    g->pos_key = pos_key;
     e = cudaGraphInstantiate(&g->exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) {
@@ -1535,7 +1445,8 @@ static int build_graph(dp_sim* s, long long steps, int kind, bool conditional, G
 
 static int get_graph(dp_sim* s, long long steps, int kind, GraphEntry** out) {
     for (auto& g : s->graphs) {
-        if (g.steps == steps && g.kind == kind && g.version == s->version) {
+        if (g.steps == steps && g.kind == kind && g.version == s->version && g.pos_key == s->pos &&
+            g.fused == use_fused_step(s)) {
             *out = &g;
             return DP_OK;
         }
@@ -1608,6 +1519,8 @@ static int run_impl(dp_sim* s, long long steps, int kind, float* ms) {
         GraphEntry* g = nullptr;
         RET(get_graph(s, c, kind, &g));
         CK(cudaGraphLaunch(g->exec, s->stream));
+        // a fused chunk of odd length leaves the positions in the other buffer set
+        if (g->fused && (c & 1)) swap_position_buffers(s);
         RET(read_status(s));
         if (s->hstat->nonfinite) {
             s->hstat->nonfinite = 0;
@@ -1654,6 +1567,10 @@ int dp_create(int dim, int64_t n, int precision, dp_sim** out) {
     s->dim = dim;
     s->n = n;
     s->precision = precision;
+    // DOMPAP_CONDITIONAL_GRAPHS=0 selects the gated rebuild kernels (profilers
+    // that do not follow conditional graph nodes see every launch then)
+    if (const char* env = std::getenv("DOMPAP_CONDITIONAL_GRAPHS")) s->conditional_graphs = std::atoi(env) != 0;
+    if (const char* env = std::getenv("DOMPAP_FUSED_STEP")) s->fused_step = std::atoi(env) != 0;
     int rc = DP_OK;
     auto cleanup = [&]() {
         dp_destroy(s);
@@ -1673,7 +1590,8 @@ int dp_create(int dim, int64_t n, int precision, dp_sim** out) {
         return cleanup();
     s->shadow_bytes = (size_t)n * (dim == 2 ? 8 : 16);
     if ((rc = dalloc(&s->shadow, s->shadow_bytes)) || (rc = dalloc(&s->shadow_ref, s->shadow_bytes)) ||
-        (rc = dalloc(&s->pos64, (size_t)n * (dim == 2 ? 16 : 32))))
+        (rc = dalloc(&s->pos64, (size_t)n * (dim == 2 ? 16 : 32))) || (rc = dalloc_t(&s->pos_alt, nd)) ||
+        (rc = dalloc(&s->shadow_alt, s->shadow_bytes)) || (rc = dalloc(&s->pos64_alt, (size_t)n * (dim == 2 ? 16 : 32))))
         return cleanup();
     if (cudaMemset(s->shadow, 0, s->shadow_bytes) != cudaSuccess ||
         cudaMemset(s->shadow_ref, 0, s->shadow_bytes) != cudaSuccess) {
@@ -1708,6 +1626,7 @@ int dp_destroy(dp_sim* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_graphs(s);
     void* bufs[] = {s->pos, s->vel, s->beta, s->force, s->pos_ref, s->img, s->shadow, s->shadow_ref, s->pos64,
+                    s->pos_alt, s->shadow_alt, s->pos64_alt,
                     s->ff_tab, s->bk_pos,
                     s->bk_vel, s->bk_beta, s->bk_img, s->mclass, s->mcoef, s->class_mass_dev, s->mass, s->types,
                     s->sig_tab, s->eps_tab, s->isig_tab, s->nl, s->cnt, s->cell_cnt, s->cell_mem, s->dstat,
@@ -1899,6 +1818,7 @@ static std::string pair_program(int dim, int precision, int pmode, bool sig_one,
     src += std::string("#define DP_SIGMA_ONE ") + (sig_one ? "1" : "0") + "\n";
     src += std::string("#define DP_EPS_ONE ") + (eps_one ? "1" : "0") + "\n";
     src += dp_src_common;
+    src += dp_src_integrate;
     if (precision == DP_PREC_MLP) src += dp_src_mlp;
     if (precision == DP_PREC_FP64) src += dp_src_ff;
     src += "\n// ---- generated pair potential ----\n";
@@ -2096,7 +2016,7 @@ int dp_sum_mv2(dp_sim* s, double* out) {
     if (!s || !out) return fail(DP_ERR_ARG, "null argument");
     const long long blocks = grid_for(s->n, kBlock);
     RET(ensure_partial(s, blocks));
-    IntArgs a;
+    dp_int_args a;
     fill_int_args(s, a, 0);
     const unsigned g = (unsigned)blocks;
 #define DP_MV2(D)                                                                                               \
@@ -2188,10 +2108,13 @@ int dp_time_kernel(dp_sim* s, int which, int reps, float* ms) {
                 k_set_rebuild<<<1, 1, 0, s->stream>>>(s->dstat);
                 return launch_rebuild(s, nullptr);
             case DP_KERNEL_SKIN: return launch_skin_check(s);
+            case DP_KERNEL_STEP:
+                if (!use_fused_step(s)) return fail(DP_ERR_ARG, "no fused step kernel in this mode");
+                return launch_step(s, DP_INT_GJF, 0, nullptr);
             default: return fail(DP_ERR_ARG, "unknown kernel");
         }
     };
-    const bool moves = which == DP_KERNEL_GJF || which == DP_KERNEL_NVE;
+    const bool moves = which == DP_KERNEL_GJF || which == DP_KERNEL_NVE || which == DP_KERNEL_STEP;
     if (moves) RET(backup_state(s));
     RET(once());  // warm-up
     CK(cudaEventRecord(s->ev0, s->stream));
@@ -2216,7 +2139,7 @@ int dp_time_forces(dp_sim* s, int reps, float* ms) { return dp_time_kernel(s, DP
 int dp_wrap(dp_sim* s) {
     if (!s) return fail(DP_ERR_ARG, "null handle");
     if (!s->have_box) return fail(DP_ERR_ARG, "box not set");
-    IntArgs a;
+    dp_int_args a;
     fill_int_args(s, a, 0);
     const unsigned g = grid_for(s->n, kBlock);
     switch (s->dim) {
@@ -2519,7 +2442,7 @@ static int batch_record(dp_batch* b, long long steps, int sample_every, int nve,
         CK(cudaEventRecord(b->join, b->stream2));
         CK(cudaStreamWaitEvent(b->stream, b->join, 0));
     }
-    k_advance_step<<<1, 1, 0, b->stream>>>(b->dstat, steps);
+    k_advance_step<<<1, 1, 0, b->stream>>>(b->dstat, steps, 0);
     CK(cudaGetLastError());
     return DP_OK;
 }

@@ -175,9 +175,8 @@ __device__ __forceinline__ ulonglong4 dp_fixed64_pack<4>(const unsigned long lon
 // Both fixed-point forms of one coordinate from the float64 product
 // p = x 2^64 / L: the 64-bit one and its upper 32 bits (the shadow). The
 // coordinate must lie in [0, L); a product rounded up to 2^64 saturates.
-// floor(p) from the bit pattern (integer shifts; this GPU issues float64
-// conversion instructions at the float64 rate): p < 1 and negative p give 0,
-// p >= 2^64 saturates.
+// floor(p) from the bit pattern (integer shifts, no float64 conversion
+// instruction): p < 1 and negative p give 0, p >= 2^64 saturates.
 __device__ __forceinline__ unsigned long long dp_fixed64_of(double p) {
     const long long b = __double_as_longlong(p);
     const int e = (int)((b >> 52) & 0x7FF) - 1023;
@@ -192,16 +191,12 @@ __device__ __forceinline__ bool dp_isfinite_bits(double x) {
     return ((unsigned long long)__double_as_longlong(x) & 0x7FF0000000000000ull) != 0x7FF0000000000000ull;
 }
 
-// Integer m with -2^22 <= m < 2^22 as a float, exactly: one integer add to
-// the bit pattern of 1.5 * 2^23 and one float subtraction.
-__device__ __forceinline__ float dp_small_int(int m) { return __int_as_float(0x4B400000 + m) - 12582912.0f; }
+// Integer m with |m| < 2^24 as a float, exactly (one 32-bit conversion
+// instruction).
+__device__ __forceinline__ float dp_small_int(int m) { return __int2float_rn(m); }
 
-// int32 -> float rounded to nearest, on the integer and FMA pipes (this GPU
-// issues conversion instructions at the float64 rate): n = h 2^16 + l with
-// h = n >> 16 and l = n & 0xFFFF exact floats; the FMA rounds h 2^16 + l once.
-__device__ __forceinline__ float dp_i2f(int n) {
-    return fmaf(dp_small_int(n >> 16), 65536.0f, dp_small_int(n & 0xFFFF));
-}
+// int32 -> float rounded to nearest.
+__device__ __forceinline__ float dp_i2f(int n) { return __int2float_rn(n); }
 
 // float -> double by moving the bits (sign, exponent rebiased, mantissa),
 // without branches: infinities and NaN keep their class, float subnormals

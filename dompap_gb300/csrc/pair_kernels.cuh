@@ -319,6 +319,33 @@ extern "C" __global__ void DP_FORCES_BOUNDS dp_forces(dp_pair_args a) {
     if (!finite) atomicExch(&a.status->nonfinite, 1);
 }
 
+#if !DP_MLP
+// One MD step of particle i in one kernel: its pair forces from this step's
+// positions (as dp_forces), then its integration, wrap, fixed-point forms and
+// skin test (dp_integrate_one) into the second set of position buffers, which
+// no thread of this launch reads. The float64 integrator work runs on the
+// float64 pipe beside the pair arithmetic of other warps, and the forces
+// never go through memory. `far` must have been cleared by the host-side
+// step sequence when the previous step wrapped every position.
+extern "C" __global__ void DP_FORCES_BOUNDS dp_step(dp_pair_args a, dp_int_args b) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool old = false, bad = false;
+    if (i < a.n) {
+        double f[DP_DIM];
+        dp_particle_sum<DP_ACC_FORCE>(a, i, f);
+#pragma unroll
+        for (int k = 0; k < DP_DIM; ++k) bad = bad || !dp_isfinite_bits(f[k]);
+        old = dp_integrate_dispatch<DP_DIM, DP_FF != 0>(b, i, f, bad);
+    }
+    const bool any_old = __any_sync(0xffffffffu, old);
+    const bool any_bad = __any_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0) {
+        if (any_old) atomicExch(&b.st->need_rebuild, 1);
+        if (any_bad) atomicExch(&b.st->nonfinite, 1);
+    }
+}
+#endif
+
 // Per-block partial sums of a scalar pair quantity (energy or virial); the
 // host-side reduction kernel adds the partials in a fixed order.
 template <int ACC>

@@ -171,6 +171,8 @@ int dp_get_stats(dp_sim *sim, dp_stats *stats);
 #define DP_KERNEL_NVE 2     /* NVE integrate + wrap + skin test             */
 #define DP_KERNEL_REBUILD 3 /* forced neighbour-list rebuild (all kernels)  */
 #define DP_KERNEL_SKIN 4    /* skin test alone                              */
+#define DP_KERNEL_STEP 5    /* fused step: pair forces + integrate + wrap + skin test
+                               (the kernel run() launches outside the surrogate mode) */
 /* Device time of `reps` back-to-back launches of one step kernel on the
  * current state (ms per launch, CUDA events on the handle's stream). The
  * integrator variants advance the state; the list is rebuilt afterwards. */

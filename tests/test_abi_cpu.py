@@ -83,9 +83,12 @@ def test_generated_source_compiles_with_nvcc(tmp_path):
     src, _ = codegen.make_pair_source(
         "4*(r**-12-r**-6) + 0.5*exp(-(r-1.5)**2/0.02) + 0.1*cos(4*r)*exp(-r)", 3.0)
     common = open(os.path.join(_build.CSRC, "dp_common.cuh")).read()
+    integ = open(os.path.join(_build.CSRC, "dp_integrate.cuh")).read()
+    ff = open(os.path.join(_build.CSRC, "dp_ff.cuh")).read()
     pair = open(os.path.join(_build.CSRC, "pair_kernels.cuh")).read()
     prog = ("#define DP_DIM 3\n#define DP_REAL double\n#define DP_REAL_IS_FLOAT 0\n#define DP_PMODE 1\n"
-            "#define DP_SIGMA_ONE 0\n#define DP_EPS_ONE 0\n#include <cstdint>\n" + common + src + pair)
+            "#define DP_SIGMA_ONE 0\n#define DP_EPS_ONE 0\n#define DP_FF 1\n#include <cstdint>\n"
+            + common + integ + ff + src + pair)
     path = tmp_path / "prog.cu"
     path.write_text(prog)
     res = subprocess.run([_build._nvcc(), *_build.ARCH, "-std=c++17", "-c", str(path), "-o", str(tmp_path / "p.o")],

@@ -1,0 +1,70 @@
+"""The fused step kernel (pair forces + integrate + wrap + skin test in one
+launch, positions double-buffered) against the separate force and integrator
+kernels: the same trajectory, G-JF and NVE, float64-parity and float32-force
+modes, with chunk lengths that leave the positions in either buffer set."""
+import numpy as np
+import pytest
+
+from gpu_helpers import config_of, sim_from_config
+
+pytestmark = pytest.mark.gpu
+
+
+def _trajectory(monkeypatch, golden_configs, tag, fused, precision, nve):
+    monkeypatch.setenv("DOMPAP_FUSED_STEP", "1" if fused else "0")
+    np.random.seed(1234)  # the Langevin seed is drawn when the Simulation is made
+    cfg = config_of(golden_configs, tag)
+    sim = sim_from_config(cfg, tag, method="cell list" if tag in ("lj500", "wahn") else "double loop",
+                          precision=precision)
+    if nve:
+        sim.set_integrator(time_step=0.002)
+        run = sim.run_leap_frog
+    else:
+        sim.set_integrator(time_step=0.004, target_temperature=1.2, temperature_damping_time=0.2)
+        run = sim.run
+    run(37)
+    for _ in range(3):
+        run(1)
+    run(20)
+    st = sim._stats()
+    return (np.array(sim.positions), np.array(sim.velocities), np.array(sim.betas),
+            np.array(sim.image_positions), int(st.steps))
+
+
+@pytest.mark.parametrize("tag", ["lj500", "wahn", "harm2d", "harm4d"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("nve", [False, True])
+def test_fused_step_matches_separate_kernels(monkeypatch, golden_configs, tag, precision, nve):
+    a = _trajectory(monkeypatch, golden_configs, tag, True, precision, nve)
+    b = _trajectory(monkeypatch, golden_configs, tag, False, precision, nve)
+    assert a[4] == b[4] == 60
+    # the same float64 operations, compiled once by NVRTC (fused) and once by
+    # nvcc (separate kernel): agreement to rounding, amplified over 60 steps
+    assert np.max(np.abs(a[0] - b[0])) <= 1e-9
+    assert np.max(np.abs(a[1] - b[1])) <= 1e-8
+    assert np.max(np.abs(a[2] - b[2])) <= 1e-8
+    assert np.array_equal(a[3], b[3])
+
+
+def test_fused_step_is_the_run_kernel(monkeypatch, golden_configs):
+    """run() launches one pair kernel per step (plus the one-thread condition
+    kernel of the rebuild node and the step counter) when fused."""
+    from dompap_gb300 import _lib
+
+    monkeypatch.setenv("DOMPAP_FUSED_STEP", "1")
+    cfg = config_of(golden_configs, "lj500")
+    sim = sim_from_config(cfg, "lj500", method="cell list")
+    sim.set_integrator(time_step=0.004, target_temperature=1.2, temperature_damping_time=0.2)
+    sim.run(10)
+    st0 = sim._stats()
+    sim.run(64)
+    st1 = sim._stats()
+    launches = int(_lib.load().dp_kernel_launches(sim._h))
+    rebuilds = int(st1.rebuilds - st0.rebuilds)
+    # list kernels per rebuild (+ the status kernel): cell list 4 + 1, all pairs 1 + 1
+    per_rebuild = 5 if st1.method_used == _lib.DP_NL_CELL else 2
+    if st1.conditional_graphs:
+        # per step: condition + dp_step; per rebuild: the list kernels; per chunk: the step counter
+        assert launches - 2 * 64 - per_rebuild * rebuilds in (1, 2)
+    else:
+        assert launches >= 2 * 64
