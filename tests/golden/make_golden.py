@@ -6,7 +6,7 @@ Run in a checkout that has the reference source next to it::
 
     python tests/golden/make_golden.py [--reference PATH]
 
-It writes ``golden_*.npz``. Every array is produced by calling the reference's
+It writes ``golden_*.npz`` and ``checkpoint_ref.csv/.toml``. Every array is produced by calling the reference's
 own functions / ``Simulation`` methods on seeded inputs; nothing here restates
 the reference's arithmetic. The fixtures are what ``tests/`` pin the oracle and
 the CUDA path against, on machines where the reference is absent.
@@ -107,11 +107,41 @@ def record_sim(out: dict, tag: str, sim, sigma=None, epsilon=None, types=None, r
           f"K<={int(counts.max())} ({time.time() - t0:.1f} s)", flush=True)
 
 
+def make_checkpoint(Simulation):
+    """The reference's own ``to_disk`` files for a small seeded 2-D binary
+    system with velocities, betas and nonzero images (checkpoint parity)."""
+    rng = np.random.default_rng(77)
+    sim = Simulation()
+    sim.set_positions(unit_cell_coordinates=((0.0, 0.0),), cells=(4, 3), lattice_constants=(1.0, 1.0))
+    n = sim.number_of_particles()
+    sim.set_masses(masses=1.0)
+    sim.set_types([0, 1] * (n // 2))
+    sim.set_density(density=0.9)
+    sim.set_pair_potential(pair_potential_str=LJ, r_cut=1.3)
+    sim.set_neighbor_list(skin=0.3, max_number_of_neighbors=64)
+    sim.set_integrator(time_step=0.002, target_temperature=0.8, temperature_damping_time=0.5)
+    sim.velocities = rng.normal(0.0, 0.7, size=sim.positions.shape)
+    sim.betas = rng.normal(0.0, 0.05, size=sim.positions.shape)
+    sim.masses = rng.uniform(0.5, 2.0, size=(n, 1))
+    sim.image_positions = rng.integers(-3, 4, size=sim.positions.shape).astype(np.int32)
+    sim.positions = sim.positions + rng.normal(0.0, 0.02, size=sim.positions.shape)
+    sim.to_disk(particle_data=os.path.join(HERE, "checkpoint_ref.csv"),
+                meta_data=os.path.join(HERE, "checkpoint_ref.toml"))
+    print("checkpoint_ref.csv / .toml:", n, "particles")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", choices=["checkpoint"], default=None,
+                    help="regenerate only the named fixture")
     args = ap.parse_args()
     dompap = import_reference(args.reference)
+    if args.only == "checkpoint":
+        from dompap import Simulation
+
+        make_checkpoint(Simulation)
+        return
     from dompap import Simulation
     from dompap import neighbor_list as rnl
     from dompap import potential as rpot
@@ -275,6 +305,7 @@ def main():
     traj["gjfinf/images"] = sim.image_positions.copy()
     np.savez_compressed(os.path.join(HERE, "golden_traj.npz"), **traj)
     print("golden_traj.npz:", len(traj), "arrays")
+    make_checkpoint(Simulation)
 
 
 if __name__ == "__main__":
