@@ -1817,6 +1817,13 @@ static std::string pair_program(int dim, int precision, int pmode, bool sig_one,
     src += "#define DP_PMODE " + std::to_string(pmode) + "\n";
     src += std::string("#define DP_SIGMA_ONE ") + (sig_one ? "1" : "0") + "\n";
     src += std::string("#define DP_EPS_ONE ") + (eps_one ? "1" : "0") + "\n";
+    // resident 256-thread CTAs per SM the fused step kernel is compiled for
+    // (register cap 65536 / (256 n) = 40): the spilled integrator tail costs
+    // less than the occupancy it buys the latency-bound pair loop (measured on
+    // GB300 against 4, 5, 7 and 8 for both modes); DOMPAP_STEP_MIN_BLOCKS overrides
+    int step_blocks = 6;
+    if (const char* env = std::getenv("DOMPAP_STEP_MIN_BLOCKS")) step_blocks = std::atoi(env);
+    src += "#define DP_STEP_MIN_BLOCKS " + std::to_string(std::max(0, std::min(8, step_blocks))) + "\n";
     src += dp_src_common;
     src += dp_src_integrate;
     if (precision == DP_PREC_MLP) src += dp_src_mlp;

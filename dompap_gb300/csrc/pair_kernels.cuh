@@ -327,7 +327,15 @@ extern "C" __global__ void DP_FORCES_BOUNDS dp_forces(dp_pair_args a) {
 // float64 pipe beside the pair arithmetic of other warps, and the forces
 // never go through memory. `far` must have been cleared by the host-side
 // step sequence when the previous step wrapped every position.
-extern "C" __global__ void DP_FORCES_BOUNDS dp_step(dp_pair_args a, dp_int_args b) {
+#ifndef DP_STEP_MIN_BLOCKS
+#define DP_STEP_MIN_BLOCKS 0
+#endif
+#if DP_STEP_MIN_BLOCKS > 0
+#define DP_STEP_BOUNDS __launch_bounds__(256, DP_STEP_MIN_BLOCKS)
+#else
+#define DP_STEP_BOUNDS __launch_bounds__(256)
+#endif
+extern "C" __global__ void DP_STEP_BOUNDS dp_step(dp_pair_args a, dp_int_args b) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     bool old = false, bad = false;
     if (i < a.n) {
