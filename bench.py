@@ -171,6 +171,11 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
+# measured by ncu on the melted state (step ~1400) of the named workload
+PROFILED_TRAFFIC_BYTES = {("harmonic3d", "step"): 303.8e6}
+
+
 def kernel_times(sim, reps=50):
     from dompap_gb300 import _lib
 
@@ -629,7 +634,10 @@ def main():
         "gpu_launches": launches,
         "e2e": {"value": float(e2e_total.item()), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": PROFILED_TRAFFIC_BYTES.get((args.workload, dominant)),
+                     "traffic_unit": "bytes per launch (ncu)",
+                     "algorithmic_bytes_per_launch": alg[dominant] * n,
                      "algorithmic_bytes_per_particle": alg[dominant]},
         "kernel_ms": kt, "mean_neighbors": mean_k, "rebuilds_in_timed_region": rebuilds,
         "conditional_rebuild_nodes": bool(st1.conditional_graphs),
