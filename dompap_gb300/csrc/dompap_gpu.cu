@@ -668,7 +668,7 @@ struct PairLib {
     cudaKernel_t forces = nullptr, energy = nullptr, virial = nullptr, laplacian = nullptr, eval = nullptr;
     cudaKernel_t step = nullptr;  // fused forces + integrate (not in the surrogate program)
     cudaKernel_t batch[4] = {nullptr, nullptr, nullptr, nullptr};  // 128, 256, 512, 1024 threads
-    cudaKernel_t forces_mlp = nullptr, energy_mlp = nullptr, virial_mlp = nullptr;
+    cudaKernel_t forces_mlp = nullptr, energy_mlp = nullptr, virial_mlp = nullptr, mlp_finish = nullptr;
 };
 
 static std::mutex g_lib_mutex;
@@ -710,6 +710,7 @@ static int compile_pair_lib(const std::string& src, PairLib* out) {
     if (src.find("#define DP_MLP 1") == std::string::npos) CK(cudaLibraryGetKernel(&pl.step, pl.lib, "dp_step"));
     if (src.find("#define DP_MLP 1") != std::string::npos) {
         CK(cudaLibraryGetKernel(&pl.forces_mlp, pl.lib, "dp_forces_mlp"));
+        CK(cudaLibraryGetKernel(&pl.mlp_finish, pl.lib, "dp_mlp_forces_finish"));
         CK(cudaLibraryGetKernel(&pl.energy_mlp, pl.lib, "dp_energy_mlp"));
         CK(cudaLibraryGetKernel(&pl.virial_mlp, pl.lib, "dp_virial_mlp"));
     }
@@ -785,6 +786,7 @@ struct dp_sim {
 
     // pair surrogate (DP_PREC_MLP)
     const dp_mlp_dev* mlp_dev = nullptr;
+    unsigned long long* mlp_fx = nullptr;  // surrogate mode: fixed-point force sums (zero between launches)
 
     // pair parameters
     int pmode = DP_PAIR_CONST;
@@ -1104,6 +1106,18 @@ static void fill_pair_args(const dp_sim* s, dp_pair_args& a, double* out) {
     }
 }
 
+// Fixed-point force sums of the surrogate pass (allocated outside any graph
+// capture: run() calls this before capturing).
+static int ensure_mlp_fx(dp_sim* s) {
+    if (s->mlp_fx) return DP_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(s->stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return fail(DP_ERR_CUDA, "surrogate force sums not allocated before capture");
+    RET(dalloc_t(&s->mlp_fx, (size_t)s->n * s->dim));
+    CK(cudaMemsetAsync(s->mlp_fx, 0, (size_t)s->n * s->dim * sizeof(unsigned long long), s->stream));
+    return DP_OK;
+}
+
 static int launch_pair(dp_sim* s, cudaKernel_t k, double* out, long long* launches) {
     dp_pair_args a;
     fill_pair_args(s, a, out);
@@ -1114,8 +1128,19 @@ static int launch_pair(dp_sim* s, cudaKernel_t k, double* out, long long* launch
         else if (k == s->lib.virial) km = s->lib.virial_mlp;
         if (!km) return fail(DP_ERR_ARG, "this quantity is not available with the pair surrogate");
         const dp_mlp_dev* mp = s->mlp_dev;
-        void* args[] = {&a, &mp};
+        unsigned long long* fx = nullptr;
+        if (km == s->lib.forces_mlp) {
+            RET(ensure_mlp_fx(s));
+            fx = s->mlp_fx;
+        }
+        void* args[] = {&a, &mp, &fx};
         CK(cudaLaunchKernel((const void*)km, dim3(grid_for(s->n, kBlock)), dim3(kBlock), args, 0, s->stream));
+        if (fx) {
+            void* fargs[] = {&a, &fx};
+            CK(cudaLaunchKernel((const void*)s->lib.mlp_finish, dim3(grid_for(s->n * s->dim, kBlock)), dim3(kBlock),
+                                fargs, 0, s->stream));
+            if (launches) *launches += 1;
+        }
     } else {
         void* args[] = {&a};
         CK(cudaLaunchKernel((const void*)k, dim3(grid_for(s->n, kBlock)), dim3(kBlock), args, 0, s->stream));
@@ -1506,6 +1531,7 @@ static int run_impl(dp_sim* s, long long steps, int kind, float* ms) {
     // make the list current (the reference checks it at the start of every step)
     RET(update_nl(s, true, nullptr));
     RET(ensure_partial(s, grid_for(s->n, kBlock)));
+    if (s->precision == DP_PREC_MLP) RET(ensure_mlp_fx(s));
     s->launches_last = 0;
     if (ms) CK(cudaEventRecord(s->ev0, s->stream));
     const long long chunk = chunk_steps(s);
@@ -1626,7 +1652,7 @@ int dp_destroy(dp_sim* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_graphs(s);
     void* bufs[] = {s->pos, s->vel, s->beta, s->force, s->pos_ref, s->img, s->shadow, s->shadow_ref, s->pos64,
-                    s->pos_alt, s->shadow_alt, s->pos64_alt,
+                    s->pos_alt, s->shadow_alt, s->pos64_alt, s->mlp_fx,
                     s->ff_tab, s->bk_pos,
                     s->bk_vel, s->bk_beta, s->bk_img, s->mclass, s->mcoef, s->class_mass_dev, s->mass, s->types,
                     s->sig_tab, s->eps_tab, s->isig_tab, s->nl, s->cnt, s->cell_cnt, s->cell_mem, s->dstat,

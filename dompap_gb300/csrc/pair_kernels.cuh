@@ -400,14 +400,26 @@ extern "C" __global__ void dp_eval_pair(const double* s_in, double* u, double* f
 // ---------------------------------------------------------------------------
 // Pair surrogate path: the generated dp_pair_* functions hold the cheap
 // terms of the potential (in float32), the network of mlp_common.cuh the
-// costly ones. A warp owns 32 particles and walks their neighbour lists in
-// lock step: each round gathers one listed pair per particle, evaluates the
-// network on the 32 values of s = r^2 as two 16-row tensor-core tiles, sends
-// each row's result back to the lane owning the particle, and adds
-//   f/r = f_cheap(r)/r + (f r)_nn / r^2,   u = u_cheap(r) + u_nn
-// for pairs inside r_cut (sigma = epsilon = 1 in this mode).
+// costly ones; sigma = epsilon = 1 in this mode. Each unique pair inside
+// r_cut is evaluated once (Newton's third law): a warp owns 32 particles, and
+// before each round every lane advances along its particle's neighbour list
+// to the next partner j > i inside r_cut, so a round's 32 network rows are
+// all real pairs (two 16-row tensor-core tiles); each row's result goes back
+// to the lane owning the pair, which adds
+//   f/r = f_cheap(r)/r + (f r)_nn / r^2,   u = u_cheap(r) + u_nn.
+// Forces: +F to i in registers, -F to j as a 64-bit fixed-point atomic add
+// (integer sums are exact, so the result does not depend on the order of the
+// atomics; 2^-32 resolution); dp_mlp_forces_finish converts the sums to float64.
+#define DP_MLP_FX_LIMIT 1073741824.0f  // 2^30: larger contributions are flagged
+
+__device__ __forceinline__ void dp_mlp_fx_add(unsigned long long* p, float v, bool& bad) {
+    bad = bad || !(fabsf(v) < DP_MLP_FX_LIMIT);
+    const float c = fminf(fmaxf(v, -DP_MLP_FX_LIMIT), DP_MLP_FX_LIMIT);
+    atomicAdd(p, (unsigned long long)__float2ll_rn(c * 4294967296.0f));
+}
+
 template <int ACC>
-__device__ __forceinline__ void dp_mlp_pass(const dp_pair_args& a, const dp_mlp_dev* mg) {
+__device__ __forceinline__ void dp_mlp_pass(const dp_pair_args& a, const dp_mlp_dev* mg, unsigned long long* fx) {
     constexpr int D = DP_DIM;
     __shared__ dp_mlp_dev m;
     __shared__ double red[32];
@@ -421,25 +433,31 @@ __device__ __forceinline__ void dp_mlp_pass(const dp_pair_args& a, const dp_mlp_
     uint32_t ui[D];
     if (active) dp_shadow_unpack<D>(sh[i], ui);
     const int c = active ? a.cnt[i] : 0;
-    int maxc = c;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) maxc = max(maxc, __shfl_xor_sync(0xffffffffu, maxc, o));
     const float rc2 = (float)(a.rcut * a.rcut);
     float f[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) f[k] = 0.0f;
     double acc = 0.0;
-    for (int kk = 0; kk < maxc; ++kk) {
+    bool bad = false;
+    int kk = 0;
+    while (true) {
+        // this lane's next unique pair inside r_cut
         bool valid = false;
+        int j = 0;
         float q = m.x_mean, df[D];
-        if (kk < c) {
-            const int j = __ldg(a.nl + (long long)kk * n + i);
+        while (kk < c && !valid) {
+            j = __ldg(a.nl + (long long)kk * n + i);
+            ++kk;
+            if (j <= i) continue;
             uint32_t uj[D];
             dp_shadow_unpack<D>(__ldg(sh + j), uj);
             const float qq = dp_shadow_q<D>(ui, uj, a.unit, df);
-            valid = qq <= rc2 && !(ACC == DP_ACC_VIRIAL && j <= i);
-            if (valid) q = qq;
+            if (qq <= rc2) {
+                valid = true;
+                q = qq;
+            }
         }
+        if (!__any_sync(0xffffffffu, valid)) break;
         float nn_u = 0.f, nn_f = 0.f;
 #pragma unroll
         for (int t = 0; t < 2; ++t) {
@@ -462,9 +480,14 @@ __device__ __forceinline__ void dp_mlp_pass(const dp_pair_args& a, const dp_mlp_
             const float fr = dp_pair_f<float>(r, rinv) * rinv + nn_f * m.f_scale * (rinv * rinv);
             if (ACC == DP_ACC_FORCE) {
 #pragma unroll
-                for (int k = 0; k < D; ++k) f[k] = fmaf(fr, df[k], f[k]);
+                for (int k = 0; k < D; ++k) {
+                    const float fk = fr * df[k];
+                    f[k] += fk;
+                    dp_mlp_fx_add(fx + (long long)k * n + j, -fk, bad);
+                }
             } else if (ACC == DP_ACC_ENERGY) {
-                acc += (double)(dp_pair_u<float>(r, rinv) + nn_u * m.u_scale);
+                // the host halves the full-list sum: a unique pair counts twice
+                acc += 2.0 * (double)(dp_pair_u<float>(r, rinv) + nn_u * m.u_scale);
             } else {
                 acc += (double)(fr * q);
             }
@@ -472,27 +495,34 @@ __device__ __forceinline__ void dp_mlp_pass(const dp_pair_args& a, const dp_mlp_
     }
     if (ACC == DP_ACC_FORCE) {
         if (active) {
-            bool finite = true;
 #pragma unroll
-            for (int k = 0; k < D; ++k) {
-                a.out[k * n + i] = (double)f[k];
-                finite = finite && isfinite(f[k]);
-            }
-            if (!finite) atomicExch(&a.status->nonfinite, 1);
+            for (int k = 0; k < D; ++k) dp_mlp_fx_add(fx + (long long)k * n + i, f[k], bad);
         }
+        if (__any_sync(0xffffffffu, bad) && lane == 0) atomicExch(&a.status->nonfinite, 1);
     } else {
         const double v = dp_block_sum(acc, red);
         if (threadIdx.x == 0) a.partial[blockIdx.x] = v;
     }
 }
 
-extern "C" __global__ void __launch_bounds__(256) dp_forces_mlp(dp_pair_args a, const dp_mlp_dev* mlp) {
-    dp_mlp_pass<DP_ACC_FORCE>(a, mlp);
+extern "C" __global__ void __launch_bounds__(256, 2) dp_forces_mlp(dp_pair_args a, const dp_mlp_dev* mlp,
+                                                                unsigned long long* fx) {
+    dp_mlp_pass<DP_ACC_FORCE>(a, mlp, fx);
 }
-extern "C" __global__ void __launch_bounds__(256) dp_energy_mlp(dp_pair_args a, const dp_mlp_dev* mlp) {
-    dp_mlp_pass<DP_ACC_ENERGY>(a, mlp);
+extern "C" __global__ void __launch_bounds__(256, 2) dp_energy_mlp(dp_pair_args a, const dp_mlp_dev* mlp,
+                                                                unsigned long long* fx) {
+    dp_mlp_pass<DP_ACC_ENERGY>(a, mlp, fx);
 }
-extern "C" __global__ void __launch_bounds__(256) dp_virial_mlp(dp_pair_args a, const dp_mlp_dev* mlp) {
-    dp_mlp_pass<DP_ACC_VIRIAL>(a, mlp);
+extern "C" __global__ void __launch_bounds__(256, 2) dp_virial_mlp(dp_pair_args a, const dp_mlp_dev* mlp,
+                                                                unsigned long long* fx) {
+    dp_mlp_pass<DP_ACC_VIRIAL>(a, mlp, fx);
+}
+
+// Fixed-point force sums -> float64 forces (SoA), and clear the sums.
+extern "C" __global__ void __launch_bounds__(256) dp_mlp_forces_finish(dp_pair_args a, unsigned long long* fx) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n * DP_DIM) return;
+    a.out[t] = (double)(long long)fx[t] * (1.0 / 4294967296.0);
+    fx[t] = 0ull;
 }
 #endif

@@ -104,6 +104,21 @@ def test_surrogate_forces_and_energy(surrogate):
     assert np.array_equal(sim.get_forces(), f64)
 
 
+def test_surrogate_forces_deterministic_and_balanced(surrogate):
+    """Each unique pair is evaluated once and its force added to both
+    particles through 64-bit fixed-point sums: repeated evaluations are
+    bit-identical, and the total force vanishes up to the float32 rounding of
+    each particle's own sum (a pair added to one side only would leave a
+    total of the order of the force magnitudes)."""
+    sim = _liquid(seed=2)
+    sim.set_pair_surrogate(surrogate)
+    f1 = sim.get_forces()
+    f2 = sim.get_forces()
+    assert np.array_equal(f1, f2)
+    assert np.max(np.abs(f1.sum(axis=0))) <= 1e-5 * np.sum(np.abs(f1))
+    assert np.max(np.abs(f1)) > 1.0
+
+
 def test_surrogate_nve_drift_and_speed(surrogate):
     from dompap_gb300 import _lib
 
