@@ -478,7 +478,7 @@ def wahnstrom_variant(seed, steps=300, warmup=20):
             "U_per_particle": sim.get_potential_energy() / n, "g_r_first_peaks": g}
 
 
-def mlp_variant(seed, dim=3, steps=20, warmup=3):
+def mlp_variant(seed, dim=3, steps=20, warmup=3, train_steps=100000):
     """The costly potential (LJ + Gaussian + cos exp, force-shifted at r_cut = 3)
     on fcc 64^3 = 1,048,576 (D=3) or 4-point 16^4 = 262,144 (D=4) at density
     0.8: surrogate training, throughput of surrogate / FP32 / FP64 generated
@@ -490,7 +490,7 @@ def mlp_variant(seed, dim=3, steps=20, warmup=3):
     pot = expensive_string(3.0)
     t0 = time.perf_counter()
     sur = PairSurrogate(pot, 3.0, r_min=0.8, n_samples=2 ** 20, seed=seed)
-    losses = sur.train()
+    losses = sur.train(steps=train_steps)
     t_train = time.perf_counter() - t0
     acc = sur.errors()
     unit, cells = (FCC, (64, 64, 64)) if dim == 3 else (BASIS_4D, (16, 16, 16, 16))
@@ -527,16 +527,19 @@ def mlp_variant(seed, dim=3, steps=20, warmup=3):
     return res
 
 
+def variant_table(args):
+    return (("fp32_force", lambda: fp32_variant(args.workload, args.seed + 7, min(args.steps, 1000), args.warmup)),
+            ("batched_4096_lj", lambda: batched_variant(args.seed + 11)),
+            ("harmonic2d", lambda: dimension_variant("harmonic2d", args.seed + 3, 500, 10)),
+            ("harmonic4d", lambda: dimension_variant("harmonic4d", args.seed + 4, 300, 10)),
+            ("wahnstrom_256000", lambda: wahnstrom_variant(args.seed + 5)),
+            ("mlp_surrogate_3d", lambda: mlp_variant(args.seed + 6, dim=3, train_steps=args.mlp_train_steps)),
+            ("mlp_surrogate_4d", lambda: mlp_variant(args.seed + 8, dim=4, train_steps=args.mlp_train_steps)))
+
+
 def variants(args, main_sim):
     out = {}
-    for name, fn in (("fp32_force", lambda: fp32_variant(args.workload, args.seed + 7, min(args.steps, 1000),
-                                                         args.warmup)),
-                     ("batched_4096_lj", lambda: batched_variant(args.seed + 11)),
-                     ("harmonic2d", lambda: dimension_variant("harmonic2d", args.seed + 3, 500, 10)),
-                     ("harmonic4d", lambda: dimension_variant("harmonic4d", args.seed + 4, 300, 10)),
-                     ("wahnstrom_256000", lambda: wahnstrom_variant(args.seed + 5)),
-                     ("mlp_surrogate_3d", lambda: mlp_variant(args.seed + 6, dim=3)),
-                     ("mlp_surrogate_4d", lambda: mlp_variant(args.seed + 8, dim=4))):
+    for name, fn in variant_table(args):
         try:
             out[name] = fn()
         except Exception as exc:  # reported, not hidden
@@ -564,10 +567,20 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--mlp-train-steps", type=int, default=100000,
+                    help="surrogate training steps (kernel timings do not depend on the weights)")
+    ap.add_argument("--only-variant", default=None,
+                    help="run one variant of the full line alone and print its JSON (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.only_variant:
+        table = dict(variant_table(args))
+        if args.only_variant not in table:
+            raise SystemExit(f"unknown variant {args.only_variant!r}; one of {sorted(table)}")
+        print(json.dumps({args.only_variant: table[args.only_variant]()}))
         return
 
     import torch
