@@ -130,6 +130,11 @@ _SIGNATURES = {
     "dp_batch_set_launch": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "dp_batch_run": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_float)]),
+    "dp_batch_set_neighbor_list": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_int]),
+    "dp_nvrtc_check": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
+                                      ctypes.POINTER(ctypes.c_int64)]),
+    "dp_batch_list_stats": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                           ctypes.POINTER(ctypes.c_int32)]),
     "dp_batch_observables": (ctypes.c_int, [_P, _D, ctypes.c_int]),
     "dp_batch_last_forces": (ctypes.c_int, [_P, _D]),
     "dp_mlp_create": (ctypes.c_int, [ctypes.POINTER(_P)]),

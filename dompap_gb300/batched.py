@@ -5,9 +5,10 @@ A Python loop of ``Simulation.run`` over many small systems is launch-bound
 every replica resident on the GPU and advances all of them with one
 persistent kernel per ``run`` (captured in a CUDA graph): each CTA takes a
 replica from a work queue, largest first, and runs all steps of it with the
-replica's positions in shared memory. Pair forces are float32 (from
-fixed-point displacements, ~1e-7 relative), integration, wrap and
-observables float64; sigma = epsilon = 1.
+replica's positions in shared memory and its Verlet list (partners within
+r_cut + skin, rebuilt when a particle moved more than skin/2) in HBM. Pair
+forces are float32 (from fixed-point displacements, ~1e-7 relative),
+integration, wrap and observables float64; sigma = epsilon = 1.
 
 The launch shape (threads per CTA for small and large replicas and the size
 split between them) is picked by ``autotune``, which times short runs of the
@@ -36,7 +37,8 @@ class ReplicaSpec:
 
 class Replicas:
     def __init__(self, specs: list[ReplicaSpec], pair_potential_str: str, r_cut: float, time_step: float = 0.005,
-                 damping_time: float = 0.1, mass: float = 1.0, seed: int | None = None):
+                 damping_time: float = 0.1, mass: float = 1.0, seed: int | None = None, skin: float = 0.45,
+                 max_number_of_neighbors: int = 0):
         if not specs:
             raise ValueError("need at least one replica")
         self.dim = int(specs[0].positions.shape[1])
@@ -68,9 +70,22 @@ class Replicas:
         seed = int(np.random.randint(0, 2**62)) if seed is None else int(seed)
         _lib.check(lib.dp_batch_set_integrator(h, float(time_step), float(damping_time), float(mass), seed))
         self.time_step, self.damping_time, self.mass = time_step, damping_time, mass
+        self.set_neighbor_list(skin, max_number_of_neighbors)
         self.set_launch(1024, 256, 512)
 
     # ---------------------------------------------------------------- running
+    def set_neighbor_list(self, skin: float = 0.45, max_number_of_neighbors: int = 0) -> None:
+        """Verlet lists per replica with partners within r_cut + skin (skin < 0:
+        the 27-cell stencil every step); max_number_of_neighbors = 0 sizes them
+        from the densest replica."""
+        _lib.check(_lib.load().dp_batch_set_neighbor_list(self._h, float(skin), int(max_number_of_neighbors)))
+        self.skin = skin
+
+    def list_stats(self) -> dict:
+        b, o, k = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int32(0)
+        _lib.check(_lib.load().dp_batch_list_stats(self._h, ctypes.byref(b), ctypes.byref(o), ctypes.byref(k)))
+        return {"builds": int(b.value), "overflowed": int(o.value), "kmax": int(k.value)}
+
     def set_launch(self, split_n: int, threads_small: int, threads_large: int) -> None:
         _lib.check(_lib.load().dp_batch_set_launch(self._h, int(split_n), int(threads_small), int(threads_large)))
         self.launch = (split_n, threads_small, threads_large)

@@ -5,12 +5,16 @@
 // Each CTA takes a replica from a work queue (largest first) and runs all
 // `steps` steps of it before taking the next, so replicas never wait on one
 // another. Per step, inside the CTA:
-//   1. cell binning in shared memory: the replica's fixed-point positions
-//      are counting-sorted into cells at least r_cut wide (no skin, no
-//      Verlet list: the cells are rebuilt every step), or kept in index
-//      order when a box has fewer than 3 cells per axis (all-pairs);
-//   2. pair forces in float32 from the fixed-point displacements (27-cell
-//      stencil), the replica's positions read from shared memory;
+//   0. skin test against the positions of the replica's last list build;
+//   1. when a build is due (or the host changed anything since): cell
+//      binning in shared memory — the fixed-point positions counting-sorted
+//      into cells at least r_cut + skin wide, or kept in index order when a
+//      box has fewer than 3 cells per axis (all pairs) — and a Verlet list per
+//      particle (16-bit local indices, column-major in HBM); a replica whose
+//      list would overflow its capacity uses the 27-cell stencil for the rest
+//      of the launch (binning every step), so no pair is ever missed;
+//   2. pair forces in float32 from the fixed-point displacements of the
+//      listed partners, the replica's positions read from shared memory;
 //   3. G-JF (or NVE) leap-frog in float64 as dompap/integrator.py:17-40, wrap
 //      as dompap/positions.py:90-98, new fixed-point position to HBM.
 // Every `sample_every` steps the CTA adds U, W and sum m v^2 of the replica to
@@ -49,19 +53,54 @@ __device__ __forceinline__ int dp_batch_block_scan(int* cnt, int nc, int* warp_t
     return carry;
 }
 
+// visit(q) for every binned slot q != slot of the (2 reach + 1)^D cells
+// around the particle in `slot` (all slots when the box has no cells). Cells
+// are at least cutoff / reach wide, so the stencil covers the cutoff sphere.
+template <int D, typename Visit>
+__device__ __forceinline__ void dp_batch_stencil(bool cells, int reach, int slot, const uint32_t* up, const int* nc,
+                                                 const int* s_start, int n, Visit& visit) {
+    if (cells) {
+        int cp[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) cp[k] = (int)__umulhi(up[k], (uint32_t)nc[k]);
+        const int span = 2 * reach + 1;
+        int stencil = 1;
+#pragma unroll
+        for (int k = 0; k < D; ++k) stencil *= span;
+        for (int s = 0; s < stencil; ++s) {
+            int rem = s, l = 0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                int cc = cp[k] + (rem % span) - reach;
+                rem /= span;
+                cc += (cc < 0) ? nc[k] : 0;
+                cc -= (cc >= nc[k]) ? nc[k] : 0;
+                l = l * nc[k] + cc;
+            }
+            const int e = s_start[l + 1];
+            for (int q = s_start[l]; q < e; ++q)
+                if (q != slot) visit(q);
+        }
+    } else {
+        for (int q = 0; q < n; ++q)
+            if (q != slot) visit(q);
+    }
+}
+
 template <int THREADS>
 __device__ __forceinline__ void dp_batch_steps(const dp_batch_args& a) {
     constexpr int D = DP_DIM;
     typedef typename dp_shadow_t<D>::type sh_t;
     extern __shared__ __align__(16) unsigned char dp_smem[];
-    sh_t* s_sh = (sh_t*)dp_smem;                                  // [max_n] positions sorted by cell
-    unsigned short* s_idx = (unsigned short*)(s_sh + a.max_n);     // [max_n] local index of each slot
+    sh_t* s_sh = (sh_t*)dp_smem;                                  // [max_n] positions (by cell while binned)
+    unsigned short* s_idx = (unsigned short*)(s_sh + a.max_n);     // [max_n] local index of each binned slot
     int* s_start = (int*)(s_idx + ((a.max_n + 7) & ~7));           // [max_cells + 1]
     int* s_cur = s_start + a.max_cells + 1;                        // [max_cells]
     __shared__ int s_rep;
     __shared__ int s_warp[32];
     __shared__ double s_red[32];
     sh_t* gsh = (sh_t*)a.shadow;
+    sh_t* gref = (sh_t*)a.shadow_ref;
     const long long ntot = a.ntot;
 
     for (;;) {
@@ -77,61 +116,122 @@ __device__ __forceinline__ void dp_batch_steps(const dp_batch_args& a) {
         int nc[D];
         bool cells = true;
         int ncell = 1;
+        // ncell < 0: cells cutoff/2 wide (5^D stencil), > 0: cutoff wide (3^D)
+        const int reach = a.ncell[r * DP_MAX_DIM] < 0 ? 2 : 1;
 #pragma unroll
         for (int k = 0; k < D; ++k) {
             L[k] = a.box[r * DP_MAX_DIM + k];
             scale[k] = 4294967296.0 / L[k];
             unit[k] = (float)(L[k] / 4294967296.0);
-            nc[k] = a.ncell[r * DP_MAX_DIM + k];
-            cells = cells && nc[k] >= 3;
+            nc[k] = abs(a.ncell[r * DP_MAX_DIM + k]);
+            cells = cells && nc[k] >= 2 * reach + 1;
             ncell *= max(nc[k], 1);
         }
         double c[5];
 #pragma unroll
         for (int t = 0; t < 5; ++t) c[t] = a.coef[r * 5 + t];
+        // list of this replica: column-major, n rows
+        uint16_t* __restrict__ nl = a.nlist ? a.nlist + off * (long long)a.kmax : nullptr;
+        bool use_list = nl != nullptr;  // cleared for the rest of the launch if the list overflows
 
         const long long step0 = a.st->step;  // advanced by the host-side graph after this launch
         for (int step = 0; step < a.steps; ++step) {
             const long long gstep = step0 + step;
             const bool sample = a.sample_every > 0 && ((gstep + 1) % a.sample_every) == 0;
-            // ---- 1. binning
-            if (cells) {
-                for (int q = threadIdx.x; q < ncell; q += THREADS) s_start[q] = 0;
-                __syncthreads();
-                for (int p = threadIdx.x; p < n; p += THREADS) {
-                    uint32_t u[D];
+            // ---- 0. list check: a build when the list is of an older
+            // generation (the host changed state or settings since) or some
+            // particle moved more than skin/2 since the build
+            bool build = false;
+            if (use_list) {
+                int moved = a.list_gen[r] != a.gen;
+                for (int p = threadIdx.x; p < n && !moved; p += THREADS) {
+                    uint32_t u[D], u0[D];
                     dp_shadow_unpack<D>(gsh[off + p], u);
-                    int l = 0;
-#pragma unroll
-                    for (int k = 0; k < D; ++k) l = l * nc[k] + (int)__umulhi(u[k], (uint32_t)nc[k]);
-                    atomicAdd(s_start + l, 1);
+                    dp_shadow_unpack<D>(gref[off + p], u0);
+                    float df[D];
+                    moved = dp_shadow_q<D>(u, u0, unit, df) > a.skin_thr2;
                 }
-                __syncthreads();
-                dp_batch_block_scan(s_start, ncell, s_warp);
-                for (int q = threadIdx.x; q < ncell; q += THREADS) s_cur[q] = s_start[q];
-                if (threadIdx.x == 0) s_start[ncell] = n;
-                __syncthreads();
-                for (int p = threadIdx.x; p < n; p += THREADS) {
-                    const sh_t v = gsh[off + p];
-                    uint32_t u[D];
-                    dp_shadow_unpack<D>(v, u);
-                    int l = 0;
-#pragma unroll
-                    for (int k = 0; k < D; ++k) l = l * nc[k] + (int)__umulhi(u[k], (uint32_t)nc[k]);
-                    const int slot = atomicAdd(s_cur + l, 1);
-                    s_sh[slot] = v;
-                    s_idx[slot] = (unsigned short)p;
-                }
-            } else {
-                for (int p = threadIdx.x; p < n; p += THREADS) {
-                    s_sh[p] = gsh[off + p];
-                    s_idx[p] = (unsigned short)p;
-                }
+                build = __syncthreads_or(moved);
             }
-            __syncthreads();
+            // ---- 1. binning (every step without a list, else for a build)
+            if (!use_list || build) {
+                if (cells) {
+                    for (int q = threadIdx.x; q < ncell; q += THREADS) s_start[q] = 0;
+                    __syncthreads();
+                    for (int p = threadIdx.x; p < n; p += THREADS) {
+                        uint32_t u[D];
+                        dp_shadow_unpack<D>(gsh[off + p], u);
+                        int l = 0;
+#pragma unroll
+                        for (int k = 0; k < D; ++k) l = l * nc[k] + (int)__umulhi(u[k], (uint32_t)nc[k]);
+                        atomicAdd(s_start + l, 1);
+                    }
+                    __syncthreads();
+                    dp_batch_block_scan(s_start, ncell, s_warp);
+                    for (int q = threadIdx.x; q < ncell; q += THREADS) s_cur[q] = s_start[q];
+                    if (threadIdx.x == 0) s_start[ncell] = n;
+                    __syncthreads();
+                    for (int p = threadIdx.x; p < n; p += THREADS) {
+                        const sh_t v = gsh[off + p];
+                        uint32_t u[D];
+                        dp_shadow_unpack<D>(v, u);
+                        int l = 0;
+#pragma unroll
+                        for (int k = 0; k < D; ++k) l = l * nc[k] + (int)__umulhi(u[k], (uint32_t)nc[k]);
+                        const int slot = atomicAdd(s_cur + l, 1);
+                        s_sh[slot] = v;
+                        s_idx[slot] = (unsigned short)p;
+                    }
+                } else {
+                    for (int p = threadIdx.x; p < n; p += THREADS) {
+                        s_sh[p] = gsh[off + p];
+                        s_idx[p] = (unsigned short)p;
+                    }
+                }
+                __syncthreads();
+            }
+            // ---- 1b. list build from the binned positions
+            if (use_list && build) {
+                bool overflow = false;
+                for (int slot = threadIdx.x; slot < n; slot += THREADS) {
+                    uint32_t up[D];
+                    dp_shadow_unpack<D>(s_sh[slot], up);
+                    const int p = s_idx[slot];
+                    int cnt = 0;
+                    auto add = [&](int q) {
+                        uint32_t uq[D];
+                        dp_shadow_unpack<D>(s_sh[q], uq);
+                        float df[D];
+                        if (dp_shadow_q<D>(up, uq, unit, df) <= a.rl2) {
+                            if (cnt < a.kmax) nl[(long long)cnt * n + p] = s_idx[q];
+                            ++cnt;
+                        }
+                    };
+                    dp_batch_stencil<D>(cells, reach, slot, up, nc, s_start, n, add);
+                    overflow = overflow || cnt > a.kmax;
+                    a.ncnt[off + p] = min(cnt, a.kmax);
+                    gref[off + p] = s_sh[slot];
+                }
+                if (__syncthreads_or(overflow)) {
+                    use_list = false;  // the binning is in place: this step uses the stencil
+                    if (threadIdx.x == 0) atomicAdd(a.list_stats + 1, 1ull);
+                } else if (threadIdx.x == 0) {
+                    atomicAdd(a.list_stats, 1ull);
+                    a.list_gen[r] = a.gen;
+                }
+                if (use_list) {
+                    // positions back in local order for the list loop
+                    for (int p = threadIdx.x; p < n; p += THREADS) s_sh[p] = gsh[off + p];
+                    __syncthreads();
+                }
+            } else if (use_list) {
+                for (int p = threadIdx.x; p < n; p += THREADS) s_sh[p] = gsh[off + p];
+                __syncthreads();
+            }
             // ---- 2. forces (float32) and 3. integration (float64)
             double accU = 0.0, accW = 0.0, accK = 0.0;
             for (int slot = threadIdx.x; slot < n; slot += THREADS) {
+                // list mode: slot = local index; stencil mode: binned slot
                 uint32_t up[D];
                 dp_shadow_unpack<D>(s_sh[slot], up);
                 float f[D];
@@ -156,33 +256,19 @@ __device__ __forceinline__ void dp_batch_steps(const dp_batch_args& a) {
                         }
                     }
                 };
-                if (cells) {
-                    int cp[D];
-#pragma unroll
-                    for (int k = 0; k < D; ++k) cp[k] = (int)__umulhi(up[k], (uint32_t)nc[k]);
-                    int stencil = 1;
-#pragma unroll
-                    for (int k = 0; k < D; ++k) stencil *= 3;
-                    for (int s = 0; s < stencil; ++s) {
-                        int rem = s, l = 0;
-#pragma unroll
-                        for (int k = 0; k < D; ++k) {
-                            int cc = cp[k] + (rem % 3) - 1;
-                            rem /= 3;
-                            cc += (cc < 0) ? nc[k] : 0;
-                            cc -= (cc >= nc[k]) ? nc[k] : 0;
-                            l = l * nc[k] + cc;
-                        }
-                        const int e = s_start[l + 1];
-                        for (int q = s_start[l]; q < e; ++q)
-                            if (q != slot) pair(q);
-                    }
+                int p;
+                if (use_list) {
+                    p = slot;
+                    const int cnt = a.ncnt[off + p];
+                    const uint16_t* __restrict__ row = nl + p;
+#pragma unroll 4
+                    for (int k = 0; k < cnt; ++k) pair(__ldg(row + (long long)k * n));
                 } else {
-                    for (int q = 0; q < n; ++q)
-                        if (q != slot) pair(q);
+                    p = s_idx[slot];
+                    dp_batch_stencil<D>(cells, reach, slot, up, nc, s_start, n, pair);
                 }
                 // integrate particle i (float64)
-                const long long i = off + s_idx[slot];
+                const long long i = off + p;
                 float z[4];
                 if (!a.nve) dp_normals4(a.seed, (unsigned long long)gstep, (uint32_t)i, z);
                 uint32_t un[D];

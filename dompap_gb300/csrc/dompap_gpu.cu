@@ -674,13 +674,8 @@ struct PairLib {
 static std::mutex g_lib_mutex;
 static std::unordered_map<std::string, PairLib> g_libs;
 
-static int compile_pair_lib(const std::string& src, PairLib* out) {
-    std::lock_guard<std::mutex> lock(g_lib_mutex);
-    auto it = g_libs.find(src);
-    if (it != g_libs.end()) {
-        *out = it->second;
-        return DP_OK;
-    }
+// NVRTC: program text -> sm_103a CUBIN (host only; no GPU needed).
+static int nvrtc_cubin(const std::string& src, std::vector<char>* cubin) {
     nvrtcProgram prog;
     nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "dompap_pair.cu", 0, nullptr, nullptr);
     if (r != NVRTC_SUCCESS) return fail(DP_ERR_NVRTC, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
@@ -697,9 +692,21 @@ static int compile_pair_lib(const std::string& src, PairLib* out) {
     }
     size_t cubin_size = 0;
     nvrtcGetCUBINSize(prog, &cubin_size);
-    std::vector<char> cubin(cubin_size);
-    nvrtcGetCUBIN(prog, cubin.data());
+    cubin->resize(cubin_size);
+    nvrtcGetCUBIN(prog, cubin->data());
     nvrtcDestroyProgram(&prog);
+    return DP_OK;
+}
+
+static int compile_pair_lib(const std::string& src, PairLib* out) {
+    std::lock_guard<std::mutex> lock(g_lib_mutex);
+    auto it = g_libs.find(src);
+    if (it != g_libs.end()) {
+        *out = it->second;
+        return DP_OK;
+    }
+    std::vector<char> cubin;
+    RET(nvrtc_cubin(src, &cubin));
     PairLib pl;
     CK(cudaLibraryLoadData(&pl.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
     CK(cudaLibraryGetKernel(&pl.forces, pl.lib, "dp_forces"));
@@ -2318,6 +2325,16 @@ struct dp_batch {
     float* force_out = nullptr;
     dp_dev_status* dstat = nullptr;
     dp_dev_status* hstat = nullptr;
+    // Verlet lists (skin < 0: cell stencil every step); skin 0.45 was the
+    // fastest of 0.2 - 0.8 for LJ replicas at T 0.7 - 2.0, dt 0.005
+    double skin = 0.45;
+    int kmax_req = 0;  // 0: from the densest replica
+    int kmax = 0;      // capacity of the allocated lists
+    uint16_t* nlist = nullptr;
+    int32_t* ncnt = nullptr;
+    void* shadow_ref = nullptr;
+    unsigned long long* list_stats = nullptr;
+    int32_t* list_gen = nullptr;  // per replica: the generation its list was built for
     std::vector<long long> h_offset;
     std::vector<double> h_box, h_temp;
     std::vector<int> h_ncell, h_order;
@@ -2363,19 +2380,30 @@ static int batch_upload_coef(dp_batch* b) {
     return DP_OK;
 }
 
+// Cells for the replica's binning, with the cutoff c = r_cut + skin (lists)
+// or r_cut (no lists). With lists (binning only for builds) c/2 wide with a
+// 5^D stencil where every axis has at least 5 of them (stored negated): fewer
+// candidates per build; otherwise, and without lists (binning every step,
+// where the loop over many sparse cells costs more), c wide with a 3^D stencil
+// (at least 3 per axis); else all pairs inside the replica.
 static int batch_configure_cells(dp_batch* b) {
     b->h_ncell.assign((size_t)b->n_rep * DP_MAX_DIM, 0);
+    const double width = b->r_cut + std::max(0.0, b->skin);
+    const int first_reach = b->skin >= 0.0 ? 2 : 1;
     for (int r = 0; r < b->n_rep; ++r) {
-        bool ok = true;
-        int nc[DP_MAX_DIM] = {0, 0, 0, 0};
-        for (int k = 0; k < b->dim; ++k) {
-            nc[k] = (int)std::floor(b->h_box[r * DP_MAX_DIM + k] / (b->r_cut * (1.0 + 1e-6)));
-            ok = ok && nc[k] >= 3;
+        for (int reach = first_reach; reach >= 1; --reach) {
+            bool ok = true;
+            int nc[DP_MAX_DIM] = {0, 0, 0, 0};
+            for (int k = 0; k < b->dim; ++k) {
+                nc[k] = (int)std::floor(b->h_box[r * DP_MAX_DIM + k] * reach / (width * (1.0 + 1e-6)));
+                ok = ok && nc[k] >= 2 * reach + 1;
+            }
+            long long cells = 1;
+            for (int k = 0; k < b->dim; ++k) cells *= std::max(nc[k], 1);
+            if (!ok || cells > 32768) continue;
+            for (int k = 0; k < b->dim; ++k) b->h_ncell[r * DP_MAX_DIM + k] = reach == 2 ? -nc[k] : nc[k];
+            break;
         }
-        long long cells = 1;
-        for (int k = 0; k < b->dim; ++k) cells *= std::max(nc[k], 1);
-        if (!ok || cells > 32768) continue;  // all pairs inside the replica
-        for (int k = 0; k < b->dim; ++k) b->h_ncell[r * DP_MAX_DIM + k] = nc[k];
     }
     CK(cudaMemcpy(b->ncell, b->h_ncell.data(), b->h_ncell.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     b->version++;
@@ -2402,7 +2430,7 @@ static void batch_buckets(const dp_batch* b, BatchBucket* out, int* nb) {
             const int r = b->h_order[q];
             bk.max_n = std::max(bk.max_n, (int)(b->h_offset[r + 1] - b->h_offset[r]));
             int cells = 1;
-            for (int k = 0; k < b->dim; ++k) cells *= std::max(b->h_ncell[r * DP_MAX_DIM + k], 1);
+            for (int k = 0; k < b->dim; ++k) cells *= std::max(std::abs(b->h_ncell[r * DP_MAX_DIM + k]), 1);
             bk.max_cells = std::max(bk.max_cells, cells);
         }
         out[(*nb)++] = bk;
@@ -2465,6 +2493,20 @@ static int batch_record(dp_batch* b, long long steps, int sample_every, int nve,
         a.dt = b->dt;
         a.rc2 = (float)(b->r_cut * b->r_cut);
         a.seed = b->seed;
+        if (b->skin >= 0.0 && b->nlist) {
+            const double rl = b->r_cut + b->skin;
+            a.nlist = b->nlist;
+            a.ncnt = b->ncnt;
+            a.shadow_ref = b->shadow_ref;
+            a.list_stats = b->list_stats;
+            a.list_gen = b->list_gen;
+            a.gen = (int)(b->version & 0x3FFFFFFF);  // a graph is captured per version
+            a.kmax = b->kmax;
+            // conservative in float32: the list reaches a little past r_cut + skin
+            // and a build comes a little before skin/2
+            a.rl2 = (float)(rl * rl * (1.0 + 1e-5));
+            a.skin_thr2 = (float)(0.25 * b->skin * b->skin * (1.0 - 1e-5));
+        }
         const int per_sm = std::max(1, std::min(2048 / k.threads, (int)((228 * 1024) / (smem + 1024))));
         const unsigned grid = (unsigned)std::max(1, std::min(k.count, sms * per_sm));
         void* args[] = {&a};
@@ -2551,7 +2593,8 @@ int dp_batch_destroy(dp_batch* b) {
     if (b->stream2) cudaStreamSynchronize(b->stream2);
     for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
     void* bufs[] = {b->pos, b->vel, b->beta, b->stage, b->img, b->rep_of, b->order, b->ncell, b->queue, b->shadow,
-                    b->offset, b->box, b->coef, b->obs, b->force_out, b->dstat};
+                    b->offset, b->box, b->coef, b->obs, b->force_out, b->dstat, b->nlist, b->ncnt, b->shadow_ref,
+                    b->list_stats, b->list_gen};
     for (void* p : bufs)
         if (p) cudaFree(p);
     if (b->hstat) cudaFreeHost(b->hstat);
@@ -2652,12 +2695,51 @@ int dp_batch_set_launch(dp_batch* b, int split_n, int threads_small, int threads
     return DP_OK;
 }
 
+// List capacity: 1.3 x the pair count of the densest replica's list sphere + 16.
+static int batch_list_capacity(const dp_batch* b) {
+    if (b->kmax_req > 0) return std::min(b->kmax_req, 65535);
+    const double rl = b->r_cut + std::max(0.0, b->skin);
+    const double pi = 3.141592653589793;
+    const double sphere = b->dim == 2 ? pi * rl * rl : (b->dim == 3 ? 4.0 / 3.0 * pi * rl * rl * rl : 0.5 * pi * pi * rl * rl * rl * rl);
+    double rho = 0.0;
+    for (int r = 0; r < b->n_rep; ++r) {
+        double vol = 1.0;
+        for (int k = 0; k < b->dim; ++k) vol *= b->h_box[r * DP_MAX_DIM + k];
+        rho = std::max(rho, (double)(b->h_offset[r + 1] - b->h_offset[r]) / vol);
+    }
+    const long long k = ((long long)std::ceil(1.3 * sphere * rho) + 16 + 7) & ~7LL;
+    return (int)std::min<long long>(std::max<long long>(k, 8), 65535);
+}
+
+static int batch_ensure_lists(dp_batch* b) {
+    if (b->skin < 0.0) return DP_OK;
+    const int k = batch_list_capacity(b);
+    if (b->nlist && k == b->kmax) return DP_OK;
+    if (b->nlist) cudaFree(b->nlist);
+    b->nlist = nullptr;
+    RET(dalloc_t(&b->nlist, (size_t)b->ntot * (size_t)k));
+    if (!b->ncnt) RET(dalloc_t(&b->ncnt, (size_t)b->ntot));
+    if (!b->shadow_ref) RET(dalloc(&b->shadow_ref, (size_t)b->ntot * (b->dim == 2 ? 8 : 16)));
+    if (!b->list_stats) {
+        RET(dalloc_t(&b->list_stats, 2));
+        CK(cudaMemset(b->list_stats, 0, 2 * sizeof(unsigned long long)));
+    }
+    if (!b->list_gen) {
+        RET(dalloc_t(&b->list_gen, (size_t)b->n_rep));
+        CK(cudaMemset(b->list_gen, 0xFF, (size_t)b->n_rep * sizeof(int32_t)));  // -1: never built
+    }
+    b->kmax = k;
+    b->version++;
+    return DP_OK;
+}
+
 int dp_batch_run(dp_batch* b, int64_t steps, int sample_every, int nve, int record_forces, float* ms) {
     if (!b) return fail(DP_ERR_ARG, "null handle");
     if (!b->have_state || !b->have_pot) return fail(DP_ERR_NOPOT, "batch state or potential not set");
     if (steps < 0 || steps > (1LL << 30)) return fail(DP_ERR_ARG, "bad step count");
     if (steps == 0) return DP_OK;
     if (record_forces && !b->force_out) RET(dalloc_t(&b->force_out, (size_t)b->ntot * b->dim));
+    RET(batch_ensure_lists(b));
     BatchGraph* g = nullptr;
     for (auto& x : b->graphs)
         if (x.steps == steps && x.sample_every == sample_every && x.nve == nve && x.record == record_forces &&
@@ -2690,6 +2772,42 @@ int dp_batch_run(dp_batch* b, int64_t steps, int sample_every, int nve, int reco
         CK(cudaMemcpy(b->dstat, b->hstat, sizeof(dp_dev_status), cudaMemcpyHostToDevice));
         return fail(DP_ERR_NONFINITE, "a position became NaN/Inf in a replica");
     }
+    return DP_OK;
+}
+
+int dp_nvrtc_check(int dim, int precision, int pair_mode, int with_batch, const char* device_source,
+                   int64_t* cubin_bytes) {
+    if (!device_source) return fail(DP_ERR_ARG, "null source");
+    if (dim < 2 || dim > 4) return fail(DP_ERR_ARG, "dimension must be 2, 3 or 4");
+    if (precision != DP_PREC_FP64 && precision != DP_PREC_FP32 && precision != DP_PREC_MLP)
+        return fail(DP_ERR_ARG, "unknown precision");
+    if (pair_mode < DP_PAIR_CONST || pair_mode > DP_PAIR_DENSE) return fail(DP_ERR_ARG, "unknown pair mode");
+    const bool one = pair_mode == DP_PAIR_CONST;
+    const std::string src = pair_program(dim, precision, pair_mode, one, one, device_source, with_batch != 0);
+    std::vector<char> cubin;
+    RET(nvrtc_cubin(src, &cubin));
+    if (cubin_bytes) *cubin_bytes = (int64_t)cubin.size();
+    return DP_OK;
+}
+
+int dp_batch_set_neighbor_list(dp_batch* b, double skin, int kmax) {
+    if (!b) return fail(DP_ERR_ARG, "null handle");
+    if (!std::isfinite(skin)) return fail(DP_ERR_ARG, "skin must be finite");
+    if (kmax < 0 || kmax > 65535) return fail(DP_ERR_ARG, "kmax must be in [0, 65535]");
+    b->skin = skin < 0.0 ? -1.0 : skin;
+    b->kmax_req = kmax;
+    b->version++;
+    if (b->have_state && b->have_pot) RET(batch_configure_cells(b));
+    return DP_OK;
+}
+
+int dp_batch_list_stats(dp_batch* b, int64_t* builds, int64_t* overflowed, int32_t* kmax) {
+    if (!b) return fail(DP_ERR_ARG, "null handle");
+    unsigned long long h[2] = {0, 0};
+    if (b->list_stats) CK(cudaMemcpy(h, b->list_stats, sizeof(h), cudaMemcpyDeviceToHost));
+    if (builds) *builds = (int64_t)h[0];
+    if (overflowed) *overflowed = (int64_t)h[1];
+    if (kmax) *kmax = b->skin < 0.0 ? 0 : b->kmax;
     return DP_OK;
 }
 

@@ -11,6 +11,7 @@ typedef unsigned int uint32_t;
 typedef long long int64_t;
 typedef unsigned long long uint64_t;
 typedef unsigned char uint8_t;
+typedef unsigned short uint16_t;
 #endif
 
 #define DP_MAX_DIM 4
@@ -89,6 +90,16 @@ struct dp_batch_args {
     float rc2;                 // r_cut^2 (float32 cut)
     int pad;
     unsigned long long seed;
+    // Verlet lists (nlist == nullptr: cell stencil every step)
+    uint16_t* nlist;           // [off * kmax + k * n + p]: local index of the k-th listed neighbour of p
+    int32_t* ncnt;             // [ntot] list lengths
+    void* shadow_ref;          // [ntot] fixed-point positions at the replica's last build
+    unsigned long long* list_stats;  // [0]: builds, [1]: replicas whose list overflowed
+    int32_t* list_gen;         // [n_rep total] generation each replica's list was built for
+    int kmax;
+    float rl2;                 // list cutoff^2 = (r_cut + skin)^2
+    float skin_thr2;           // (skin / 2)^2: rebuild when some particle moved farther
+    int gen;                   // current generation (changes whenever the host changes state or settings)
 };
 
 // ---------------------------------------------------------------------------

@@ -226,6 +226,22 @@ int dp_batch_set_launch(dp_batch *batch, int split_n, int threads_small, int thr
  * to its observables. record_forces keeps the last step's float32 forces.
  * ms (may be NULL) receives the device time. */
 int dp_batch_run(dp_batch *batch, int64_t steps, int sample_every, int nve, int record_forces, float *ms);
+/* Compile the pair program of (dim, precision, pair mode, batch kernels) for
+ * a generated potential with NVRTC and discard it: a host-only check of the
+ * device code (no GPU needed; no counterpart in the reference). cubin_bytes
+ * (may be NULL) receives the CUBIN size. */
+int dp_nvrtc_check(int dim, int precision, int pair_mode, int with_batch, const char *device_source,
+                   int64_t *cubin_bytes);
+/* Verlet lists for the batch (replaces the per-step 27-cell stencil; no
+ * counterpart in the reference, whose replicas each run dompap's own list,
+ * dompap/neighbor_list.py:7-201): partners within r_cut + skin, rebuilt per
+ * replica when a particle moved more than skin/2 and at the start of every
+ * run. kmax = 0 sizes the lists from the densest replica; a replica whose list
+ * would overflow uses the stencil for the rest of that run. skin < 0 turns the
+ * lists off. Default: skin 0.45, kmax 0. */
+int dp_batch_set_neighbor_list(dp_batch *batch, double skin, int kmax);
+/* List builds and overflowed replicas since creation, and the list capacity in use. */
+int dp_batch_list_stats(dp_batch *batch, int64_t *builds, int64_t *overflowed, int32_t *kmax);
 /* (n_rep, 4): sum of U, sum of W, sum of sum m v^2, number of samples. reset != 0 zeroes them. */
 int dp_batch_observables(dp_batch *batch, double *out, int reset);
 /* (sum N, D) forces of the last recorded step (float32 values). */

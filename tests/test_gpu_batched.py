@@ -137,3 +137,34 @@ def test_batched_autotune_and_full_shape():
     assert np.all(np.isfinite(pos)) and np.all(pos >= 0)
     for r in range(reps.n_rep):
         assert np.all(pos[reps.replica_slice(r)] <= reps.boxes[r])
+
+
+def _run_batch(skin, kmax=0, steps=30, seed=4):
+    from dompap_gb300.batched import Replicas
+
+    specs, _ = small_specs(seed=seed, n_rep=12)
+    reps = Replicas(specs, LJ, 2.5, time_step=0.005, damping_time=0.1, seed=9, skin=skin,
+                    max_number_of_neighbors=kmax)
+    reps.run(steps)
+    pos, vel, img = reps.state()
+    return pos, vel, img, reps.list_stats()
+
+
+def test_batched_lists_match_stencil():
+    """Verlet lists (rebuilt on the skin test) and the 27-cell stencil every
+    step give the same trajectory: the same pairs, float32 sums in another order."""
+    pa, va, ia, st = _run_batch(0.3)
+    pb, vb, ib, _ = _run_batch(-1.0)
+    assert st["builds"] >= 12 and st["overflowed"] == 0 and st["kmax"] > 0
+    assert np.array_equal(ia, ib)
+    assert np.max(np.abs(pa - pb)) <= 1e-4
+    assert np.max(np.abs(va - vb)) <= 1e-3
+
+
+def test_batched_list_overflow_falls_back_to_stencil():
+    """A list capacity far below the pair count: every replica's first build
+    overflows, is counted, and the replica uses the stencil (no pair lost)."""
+    pa, va, ia, st = _run_batch(0.3, kmax=8, steps=10)
+    pb, vb, ib, _ = _run_batch(-1.0, steps=10)
+    assert st["overflowed"] == 12 and st["kmax"] == 8
+    assert np.max(np.abs(pa - pb)) <= 1e-5
