@@ -42,7 +42,8 @@ def write_embedded() -> str:
     parts = []
     for name, sym in (("dp_common.cuh", "dp_src_common"), ("pair_kernels.cuh", "dp_src_pair"),
                       ("batch_kernels.cuh", "dp_src_batch"), ("mlp_common.cuh", "dp_src_mlp"),
-                      ("dp_ff.cuh", "dp_src_ff"), ("dp_integrate.cuh", "dp_src_integrate")):
+                      ("dp_ff.cuh", "dp_src_ff"), ("dp_integrate.cuh", "dp_src_integrate"),
+                      ("dp_umma.cuh", "dp_src_umma")):
         with open(os.path.join(CSRC, name)) as fh:
             text = fh.read()
         if ')DPSRC"' in text:

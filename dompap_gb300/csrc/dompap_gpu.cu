@@ -669,6 +669,7 @@ struct PairLib {
     cudaKernel_t step = nullptr;  // fused forces + integrate (not in the surrogate program)
     cudaKernel_t batch[4] = {nullptr, nullptr, nullptr, nullptr};  // 128, 256, 512, 1024 threads
     cudaKernel_t forces_mlp = nullptr, energy_mlp = nullptr, virial_mlp = nullptr, mlp_finish = nullptr;
+    cudaKernel_t forces_mlp_tc = nullptr, energy_mlp_tc = nullptr, virial_mlp_tc = nullptr;  // tcgen05
 };
 
 static std::mutex g_lib_mutex;
@@ -718,6 +719,9 @@ static int compile_pair_lib(const std::string& src, PairLib* out) {
     if (src.find("#define DP_MLP 1") != std::string::npos) {
         CK(cudaLibraryGetKernel(&pl.forces_mlp, pl.lib, "dp_forces_mlp"));
         CK(cudaLibraryGetKernel(&pl.mlp_finish, pl.lib, "dp_mlp_forces_finish"));
+        CK(cudaLibraryGetKernel(&pl.forces_mlp_tc, pl.lib, "dp_forces_mlp_tc"));
+        CK(cudaLibraryGetKernel(&pl.energy_mlp_tc, pl.lib, "dp_energy_mlp_tc"));
+        CK(cudaLibraryGetKernel(&pl.virial_mlp_tc, pl.lib, "dp_virial_mlp_tc"));
         CK(cudaLibraryGetKernel(&pl.energy_mlp, pl.lib, "dp_energy_mlp"));
         CK(cudaLibraryGetKernel(&pl.virial_mlp, pl.lib, "dp_virial_mlp"));
     }
@@ -754,6 +758,10 @@ struct dp_sim {
     cudaStream_t cstream = nullptr;  // captures the bodies of conditional graph nodes
     bool conditional_graphs = true;  // cleared if the driver rejects conditional nodes
     bool fused_step = true;          // run() uses dp_step (DOMPAP_FUSED_STEP=0: separate kernels)
+    // surrogate pass: 0 = tcgen05 from 65,536 particles (the 128-particle CTAs
+    // fill the GPU; on par with mma.sync there), mma.sync below; 1 = tcgen05;
+    // 2 = mma.sync (DOMPAP_MLP_TENSOR=tcgen05 | mma)
+    int mlp_tensor = 0;
     // second set of position buffers: a fused step reads pos/shadow/pos64 and
     // writes these, then the two sets change roles
     double* pos_alt = nullptr;
@@ -1113,6 +1121,10 @@ static void fill_pair_args(const dp_sim* s, dp_pair_args& a, double* out) {
     }
 }
 
+static bool use_mlp_tcgen05(const dp_sim* s) {
+    return s->mlp_tensor == 1 || (s->mlp_tensor == 0 && s->n >= 65536);
+}
+
 // Fixed-point force sums of the surrogate pass (allocated outside any graph
 // capture: run() calls this before capturing).
 static int ensure_mlp_fx(dp_sim* s) {
@@ -1141,7 +1153,14 @@ static int launch_pair(dp_sim* s, cudaKernel_t k, double* out, long long* launch
             fx = s->mlp_fx;
         }
         void* args[] = {&a, &mp, &fx};
-        CK(cudaLaunchKernel((const void*)km, dim3(grid_for(s->n, kBlock)), dim3(kBlock), args, 0, s->stream));
+        if (use_mlp_tcgen05(s)) {
+            // the tcgen05 pass: 128 particles (rows of the tensor-core tile) per CTA
+            cudaKernel_t kt = km == s->lib.forces_mlp ? s->lib.forces_mlp_tc
+                            : (km == s->lib.energy_mlp ? s->lib.energy_mlp_tc : s->lib.virial_mlp_tc);
+            CK(cudaLaunchKernel((const void*)kt, dim3(grid_for(s->n, 128)), dim3(128), args, 0, s->stream));
+        } else {
+            CK(cudaLaunchKernel((const void*)km, dim3(grid_for(s->n, kBlock)), dim3(kBlock), args, 0, s->stream));
+        }
         if (fx) {
             void* fargs[] = {&a, &fx};
             CK(cudaLaunchKernel((const void*)s->lib.mlp_finish, dim3(grid_for(s->n * s->dim, kBlock)), dim3(kBlock),
@@ -1261,6 +1280,16 @@ static int read_status(dp_sim* s) {
     CK(cudaMemcpyAsync(s->hstat, s->dstat, sizeof(dp_dev_status), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return DP_OK;
+}
+
+// A bounded device-side wait gave up (the tensor-core surrogate pass): the
+// launch's results are invalid; report it and clear the flag.
+static int write_status(dp_sim* s);
+static int check_device_error(dp_sim* s) {
+    if (!s->hstat->device_error) return DP_OK;
+    s->hstat->device_error = 0;
+    RET(write_status(s));
+    return fail(DP_ERR_CUDA, "a device-side wait timed out in the tensor-core surrogate pass");
 }
 
 static int write_status(dp_sim* s) {
@@ -1555,6 +1584,7 @@ static int run_impl(dp_sim* s, long long steps, int kind, float* ms) {
         // a fused chunk of odd length leaves the positions in the other buffer set
         if (g->fused && (c & 1)) swap_position_buffers(s);
         RET(read_status(s));
+        RET(check_device_error(s));
         if (s->hstat->nonfinite) {
             s->hstat->nonfinite = 0;
             RET(write_status(s));
@@ -1604,6 +1634,8 @@ int dp_create(int dim, int64_t n, int precision, dp_sim** out) {
     // that do not follow conditional graph nodes see every launch then)
     if (const char* env = std::getenv("DOMPAP_CONDITIONAL_GRAPHS")) s->conditional_graphs = std::atoi(env) != 0;
     if (const char* env = std::getenv("DOMPAP_FUSED_STEP")) s->fused_step = std::atoi(env) != 0;
+    if (const char* env = std::getenv("DOMPAP_MLP_TENSOR"))
+        s->mlp_tensor = std::strcmp(env, "tcgen05") == 0 ? 1 : (std::strcmp(env, "mma") == 0 ? 2 : 0);
     int rc = DP_OK;
     auto cleanup = [&]() {
         dp_destroy(s);
@@ -1860,6 +1892,7 @@ static std::string pair_program(int dim, int precision, int pmode, bool sig_one,
     src += dp_src_common;
     src += dp_src_integrate;
     if (precision == DP_PREC_MLP) src += dp_src_mlp;
+    if (precision == DP_PREC_MLP) src += dp_src_umma;
     if (precision == DP_PREC_FP64) src += dp_src_ff;
     src += "\n// ---- generated pair potential ----\n";
     src += pot_src;
@@ -2006,6 +2039,7 @@ int dp_forces(dp_sim* s, double* forces) {
     RET(update_nl(s, true, nullptr));
     RET(launch_pair(s, s->lib.forces, s->force, nullptr));
     RET(read_status(s));
+    RET(check_device_error(s));
     if (s->hstat->nonfinite) {
         s->hstat->nonfinite = 0;
         RET(write_status(s));
@@ -2017,7 +2051,9 @@ static int scalar_pair(dp_sim* s, cudaKernel_t k, double* out) {
     RET(require_ready(s));
     if (!out) return fail(DP_ERR_ARG, "null output");
     RET(update_nl(s, true, nullptr));
-    const long long blocks = grid_for(s->n, kBlock);
+    // one partial sum per block of the kernel launch_pair uses
+    const bool tc = s->precision == DP_PREC_MLP && use_mlp_tcgen05(s);
+    const long long blocks = grid_for(s->n, tc ? 128 : kBlock);
     RET(ensure_partial(s, blocks));
     RET(launch_pair(s, k, nullptr, nullptr));
     k_reduce<<<1, 1024, 0, s->stream>>>(s->partial, blocks, s->dsum);
@@ -2025,6 +2061,10 @@ static int scalar_pair(dp_sim* s, cudaKernel_t k, double* out) {
     CK(cudaMemcpyAsync(s->hsum, s->dsum, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     *out = *s->hsum;
+    if (tc) {
+        RET(read_status(s));
+        RET(check_device_error(s));
+    }
     return DP_OK;
 }
 

@@ -518,6 +518,215 @@ extern "C" __global__ void __launch_bounds__(256, 2) dp_virial_mlp(dp_pair_args 
     dp_mlp_pass<DP_ACC_VIRIAL>(a, mlp, fx);
 }
 
+// ---------------------------------------------------------------------------
+// The same pass on the fifth-generation tensor cores (dp_umma.cuh): a CTA of
+// 128 threads owns 128 particles; per round every thread takes its next unique
+// pair inside r_cut and writes that pair's layer-1 activations (bf16 high part
+// and remainder) as one row of the 128 x 64 A operand in shared memory; one
+// thread issues the 4 K-steps x 2 parts of tcgen05.mma against W2 (bf16, in
+// shared memory) into a 128-lane x 64-column fp32 TMEM accumulator; each thread
+// then reads its own row back (tcgen05.ld) and finishes layers 2 and 3 for its
+// pair, with no exchange between threads.
+#define DP_TC_WAIT_LIMIT (1 << 22)
+
+template <int ACC>
+__device__ __forceinline__ void dp_mlp_pass_tc(const dp_pair_args& a, const dp_mlp_dev* mg, unsigned long long* fx) {
+    constexpr int D = DP_DIM;
+    constexpr int ROWS = 128;
+    __shared__ __align__(128) unsigned char sA_hi[ROWS * 64 * 2];
+    __shared__ __align__(128) unsigned char sA_lo[ROWS * 64 * 2];
+    __shared__ __align__(128) unsigned char sB[64 * 64 * 2];
+    __shared__ float s_w1[64], s_b1[64], s_b2[64], s_w30[64], s_w31[64], s_misc[6];
+    __shared__ __align__(8) uint64_t s_mbar;
+    __shared__ uint32_t s_tmem;
+    __shared__ double red[32];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // network: scalars, and W2 from its packed B fragments into the canonical layout
+    if (tid < 64) {
+        s_w1[tid] = mg->w1[tid];
+        s_b1[tid] = mg->b1[tid];
+        s_b2[tid] = mg->b2[tid];
+        s_w30[tid] = mg->w3[0][tid];
+        s_w31[tid] = mg->w3[1][tid];
+    }
+    if (tid == 0) {
+        s_misc[0] = mg->b3[0];
+        s_misc[1] = mg->b3[1];
+        s_misc[2] = mg->x_mean;
+        s_misc[3] = mg->x_inv_scale;
+        s_misc[4] = mg->u_scale;
+        s_misc[5] = mg->f_scale;
+        dp_mbar_init(&s_mbar, 1);
+    }
+    for (int t = tid; t < 4 * 8 * 32; t += ROWS) {
+        const int lane = t & 31, nt = (t >> 5) & 7, kt = t >> 8;
+        const int nrow = nt * 8 + (lane >> 2), k = kt * 16 + 2 * (lane & 3);
+        *(uint32_t*)(sB + dp_umma_offset(nrow, k, 64)) = mg->w2frag[t * 2 + 0];
+        *(uint32_t*)(sB + dp_umma_offset(nrow, k + 8, 64)) = mg->w2frag[t * 2 + 1];
+    }
+    if (warp == 0) dp_tmem_alloc(&s_tmem, 64);
+    dp_async_smem_fence();
+    dp_tc_fence_before();
+    __syncthreads();
+    dp_tc_fence_after();
+    const uint32_t tmem = s_tmem;
+    const uint32_t idesc = dp_umma_idesc_bf16<ROWS, 64>();
+    const float x_mean = s_misc[2], x_inv = s_misc[3], u_scale = s_misc[4], f_scale = s_misc[5];
+
+    const long long n = a.n;
+    const long long i = (long long)blockIdx.x * ROWS + tid;
+    const bool active = i < n;
+    const shadow_t* __restrict__ sh = (const shadow_t*)a.shadow;
+    uint32_t ui[D];
+    if (active) dp_shadow_unpack<D>(sh[i], ui);
+    const int c = active ? a.cnt[i] : 0;
+    const float rc2 = (float)(a.rcut * a.rcut);
+    float f[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) f[k] = 0.0f;
+    double acc = 0.0;
+    bool bad = false, timed_out = false;
+    uint32_t phase = 0;
+    int kk = 0;
+    // this thread's next unique pair inside r_cut (the search of round r + 1
+    // runs while the tensor core computes round r)
+    bool nvalid = false;
+    int nj = 0;
+    float nq = x_mean;
+    auto search = [&]() {
+        nvalid = false;
+        nq = x_mean;
+        while (kk < c && !nvalid) {
+            const int jj = __ldg(a.nl + (long long)kk * n + i);
+            ++kk;
+            if (jj <= i) continue;
+            uint32_t uj[D];
+            dp_shadow_unpack<D>(__ldg(sh + jj), uj);
+            float dd[D];
+            const float qq = dp_shadow_q<D>(ui, uj, a.unit, dd);
+            if (qq <= rc2) {
+                nvalid = true;
+                nj = jj;
+                nq = qq;
+            }
+        }
+    };
+    search();
+    while (true) {
+        const bool valid = nvalid;
+        const int j = nj;
+        const float q = nq;
+        // previous round's TMEM reads are complete in every thread past this barrier
+        dp_tc_fence_before();
+        if (!__syncthreads_or(valid)) break;
+        dp_tc_fence_after();
+        // layer 1 into row tid of the A operand
+        const float x = (q - x_mean) * x_inv;
+#pragma unroll
+        for (int g8 = 0; g8 < 8; ++g8) {
+            uint32_t hi[4], lo[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int k = g8 * 8 + 2 * e;
+                dp_split2(dp_mlp_act<false>(fmaf(s_w1[k], x, s_b1[k])),
+                          dp_mlp_act<false>(fmaf(s_w1[k + 1], x, s_b1[k + 1])), hi[e], lo[e]);
+            }
+            const int o = dp_umma_offset(tid, g8 * 8, ROWS);
+            *(uint4*)(sA_hi + o) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+            *(uint4*)(sA_lo + o) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+        }
+        dp_async_smem_fence();
+        dp_tc_fence_before();
+        __syncthreads();
+        dp_tc_fence_after();
+        if (tid == 0) {
+            const uint32_t a_hi = dp_smem_addr(sA_hi), a_lo = dp_smem_addr(sA_lo), b = dp_smem_addr(sB);
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+                const uint64_t bd = dp_umma_desc(b + ks * (64 * 32));
+                dp_umma_bf16(tmem, dp_umma_desc(a_lo + ks * (ROWS * 32)), bd, idesc, ks > 0 ? 1u : 0u);
+                dp_umma_bf16(tmem, dp_umma_desc(a_hi + ks * (ROWS * 32)), bd, idesc, 1u);
+            }
+            dp_umma_commit(&s_mbar);
+        }
+        search();  // next round's pair, overlapping the MMAs
+        const bool ok = dp_mbar_wait(&s_mbar, phase, DP_TC_WAIT_LIMIT);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            timed_out = true;
+            break;
+        }
+        dp_tc_fence_after();
+        // layers 2 and 3 for this thread's pair: two halves of 32 columns
+        float y0 = s_misc[0], y1 = s_misc[1];
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            float z[32];
+            dp_tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(half * 32), z);
+#pragma unroll
+            for (int cc = 0; cc < 32; ++cc) {
+                const int col = half * 32 + cc;
+                const float h = dp_mlp_act<false>(z[cc] + s_b2[col]);
+                y0 = fmaf(h, s_w30[col], y0);
+                y1 = fmaf(h, s_w31[col], y1);
+            }
+        }
+        if (valid) {
+            const float rinv = rsqrtf(q);
+            const float r = q * rinv;
+            const float fr = dp_pair_f<float>(r, rinv) * rinv + y1 * f_scale * (rinv * rinv);
+            if (ACC == DP_ACC_FORCE) {
+                // the displacement again from the partner's shadow (cached), not kept across the round
+                uint32_t uj[D];
+                dp_shadow_unpack<D>(__ldg(sh + j), uj);
+                float df[D];
+                dp_shadow_q<D>(ui, uj, a.unit, df);
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    const float fk = fr * df[k];
+                    f[k] += fk;
+                    dp_mlp_fx_add(fx + (long long)k * n + j, -fk, bad);
+                }
+            } else if (ACC == DP_ACC_ENERGY) {
+                acc += 2.0 * (double)(dp_pair_u<float>(r, rinv) + y0 * u_scale);
+            } else {
+                acc += (double)(fr * q);
+            }
+        }
+    }
+    if (timed_out) {
+        // the MMAs of the abandoned round may still be in flight: wait (bounded) before freeing TMEM
+        dp_mbar_wait(&s_mbar, phase ^ 1u, DP_TC_WAIT_LIMIT);
+        if (tid == 0) atomicExch(&a.status->device_error, 1);
+    }
+    dp_tc_fence_before();
+    __syncthreads();
+    if (warp == 0) dp_tmem_dealloc(tmem, 64);
+    if (ACC == DP_ACC_FORCE) {
+        if (active) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) dp_mlp_fx_add(fx + (long long)k * n + i, f[k], bad);
+        }
+        if (bad) atomicExch(&a.status->nonfinite, 1);
+    } else {
+        const double v = dp_block_sum(acc, red);
+        if (threadIdx.x == 0) a.partial[blockIdx.x] = v;
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(128, 5) dp_forces_mlp_tc(dp_pair_args a, const dp_mlp_dev* mlp,
+                                                                      unsigned long long* fx) {
+    dp_mlp_pass_tc<DP_ACC_FORCE>(a, mlp, fx);
+}
+extern "C" __global__ void __launch_bounds__(128, 5) dp_energy_mlp_tc(dp_pair_args a, const dp_mlp_dev* mlp,
+                                                                      unsigned long long* fx) {
+    dp_mlp_pass_tc<DP_ACC_ENERGY>(a, mlp, fx);
+}
+extern "C" __global__ void __launch_bounds__(128, 5) dp_virial_mlp_tc(dp_pair_args a, const dp_mlp_dev* mlp,
+                                                                      unsigned long long* fx) {
+    dp_mlp_pass_tc<DP_ACC_VIRIAL>(a, mlp, fx);
+}
+
 // Fixed-point force sums -> float64 forces (SoA), and clear the sums.
 extern "C" __global__ void __launch_bounds__(256) dp_mlp_forces_finish(dp_pair_args a, unsigned long long* fx) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;

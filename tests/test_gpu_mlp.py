@@ -119,6 +119,26 @@ def test_surrogate_forces_deterministic_and_balanced(surrogate):
     assert np.max(np.abs(f1)) > 1.0
 
 
+def test_tcgen05_pass_matches_mma_sync_pass(surrogate, monkeypatch):
+    """The surrogate's 128 x 64 x 64 layer on the fifth-generation tensor
+    cores (tcgen05.mma, TMEM accumulator) and on mma.sync give the same
+    forces, energy and virial: the same bf16 operands and fp32 accumulation,
+    summed in another order."""
+    out = {}
+    for tag, env in (("tc", "tcgen05"), ("mma", "mma")):
+        monkeypatch.setenv("DOMPAP_MLP_TENSOR", env)
+        sim = _liquid(seed=3)
+        sim.set_pair_surrogate(surrogate)
+        out[tag] = (sim.get_forces(), sim.get_potential_energy(), sim.get_virial())
+    f_tc, u_tc, w_tc = out["tc"]
+    f_mm, u_mm, w_mm = out["mma"]
+    err = np.sqrt(np.mean((f_tc - f_mm) ** 2) / np.mean(f_mm ** 2))
+    print(f"tcgen05 vs mma.sync: force relative RMS {err:.2e}, U {u_tc:.9f} vs {u_mm:.9f}, W {w_tc:.9f} vs {w_mm:.9f}")
+    assert err <= 1e-5
+    assert abs(u_tc - u_mm) <= 1e-6 * abs(u_mm)
+    assert abs(w_tc - w_mm) <= 1e-6 * abs(w_mm)
+
+
 def test_surrogate_nve_drift_and_speed(surrogate):
     from dompap_gb300 import _lib
 
