@@ -1869,7 +1869,7 @@ static std::string hexd(double v) {
 }
 
 static std::string pair_program(int dim, int precision, int pmode, bool sig_one, bool eps_one,
-                                const std::string& pot_src, bool with_batch) {
+                                const std::string& pot_src, bool with_batch, int step_blocks_hint = 6) {
     std::string src;
     src += "#define DP_DIM " + std::to_string(dim) + "\n";
     if (precision == DP_PREC_MLP) src += "#define DP_MLP 1\n";
@@ -1883,10 +1883,8 @@ static std::string pair_program(int dim, int precision, int pmode, bool sig_one,
     src += std::string("#define DP_SIGMA_ONE ") + (sig_one ? "1" : "0") + "\n";
     src += std::string("#define DP_EPS_ONE ") + (eps_one ? "1" : "0") + "\n";
     // resident 256-thread CTAs per SM the fused step kernel is compiled for
-    // (register cap 65536 / (256 n) = 40): the spilled integrator tail costs
-    // less than the occupancy it buys the latency-bound pair loop (measured on
-    // GB300 against 4, 5, 7 and 8 for both modes); DOMPAP_STEP_MIN_BLOCKS overrides
-    int step_blocks = 6;
+    // (register cap 65536 / (256 n)); DOMPAP_STEP_MIN_BLOCKS overrides
+    int step_blocks = step_blocks_hint;
     if (const char* env = std::getenv("DOMPAP_STEP_MIN_BLOCKS")) step_blocks = std::atoi(env);
     src += "#define DP_STEP_MIN_BLOCKS " + std::to_string(std::max(0, std::min(8, step_blocks))) + "\n";
     src += dp_src_common;
@@ -1905,10 +1903,18 @@ static std::string pair_program(int dim, int precision, int pmode, bool sig_one,
     return src;
 }
 
+// The fused step kernel is compiled for 6 resident 256-thread CTAs per SM (40
+// registers) with constant sigma/epsilon: there the spilled integrator tail
+// (~240 bytes) costs less than the occupancy buys (measured on GB300 against
+// 4, 5, 7 and 8). With per-type or per-pair tables the pair loop spills
+// ~600 bytes under that cap (the Wahnstrom mixture ran 17 % slower), so those
+// use 4 (64 registers).
 static int rebuild_pair_lib(dp_sim* s) {
     const bool sig_one = s->pmode == DP_PAIR_CONST && s->sigma == 1.0;
     const bool eps_one = s->pmode == DP_PAIR_CONST && s->epsilon == 1.0;
-    const std::string src = pair_program(s->dim, s->precision, s->pmode, sig_one, eps_one, s->pot_src, false);
+    const int step_blocks = s->pmode == DP_PAIR_CONST ? 6 : 4;
+    const std::string src =
+        pair_program(s->dim, s->precision, s->pmode, sig_one, eps_one, s->pot_src, false, step_blocks);
     PairLib pl;
     RET(compile_pair_lib(src, &pl));
     s->lib = pl;
