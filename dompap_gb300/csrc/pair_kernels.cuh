@@ -412,10 +412,22 @@ extern "C" __global__ void dp_eval_pair(const double* s_in, double* u, double* f
 // atomics; 2^-32 resolution); dp_mlp_forces_finish converts the sums to float64.
 #define DP_MLP_FX_LIMIT 1073741824.0f  // 2^30: larger contributions are flagged
 
+// round(v 2^32) for |v| <= 2^30 from the float's bits (integer shifts, no
+// 64-bit conversion instruction); halves round away from zero.
+__device__ __forceinline__ long long dp_f2fx32(float v) {
+    const uint32_t b = __float_as_uint(v);
+    const int e = (int)((b >> 23) & 0xFFu) - 127;  // v = 1.m 2^e
+    if (e < -33) return 0;                          // |v 2^32| < 1/2 (zeros and subnormals too)
+    const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u);
+    const int sh = e + 9;                           // v 2^32 = m 2^(e + 32 - 23)
+    const long long r = sh >= 0 ? (m << sh) : ((m + (1LL << (-sh - 1))) >> (-sh));
+    return (b >> 31) ? -r : r;
+}
+
 __device__ __forceinline__ void dp_mlp_fx_add(unsigned long long* p, float v, bool& bad) {
     bad = bad || !(fabsf(v) < DP_MLP_FX_LIMIT);
     const float c = fminf(fmaxf(v, -DP_MLP_FX_LIMIT), DP_MLP_FX_LIMIT);
-    atomicAdd(p, (unsigned long long)__float2ll_rn(c * 4294967296.0f));
+    atomicAdd(p, (unsigned long long)dp_f2fx32(c));
 }
 
 template <int ACC>
