@@ -173,7 +173,8 @@ __global__ void k_skin_check(SkinArgs a) {
         double x[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) x[k] = a.pos[k * a.n + i];
-        old = dp_skin_old<D>(a.shadow_ref, a.pos_ref, a.n, a.unit, a.box, a.thr, a.thr_lo, a.thr_hi, i, u, x);
+        old = dp_skin_old<D>(a.shadow_ref, a.pos_ref, a.n, a.unit, a.box, a.thr, a.thr_lo, a.thr_hi, i, u, x,
+                             a.st->far != 0 || a.st->ref_far != 0);
     }
     if (__any_sync(0xffffffffu, old) && (threadIdx.x & 31) == 0) atomicExch(&a.st->need_rebuild, 1);
 }
@@ -402,6 +403,7 @@ __global__ void k_rebuild_done(dp_dev_status* st) {
     if (st->need_rebuild) {
         st->need_rebuild = 0;
         st->rebuilds += 1;
+        st->ref_far = st->far;  // the list's reference positions are the current ones
     }
 }
 

@@ -25,6 +25,8 @@ struct dp_dev_status {
     int32_t nonfinite;        // a force or position became NaN/Inf
     int32_t far;              // some coordinate lies outside [-L/4, 5L/4) (not yet wrapped)
     int32_t device_error;     // a bounded device-side wait gave up: the launch's results are invalid
+    int32_t ref_far;          // `far` held when the current list was built (its reference positions)
+    int32_t pad;
     int64_t rebuilds;         // neighbour-list builds done on the device
     int64_t step;             // steps integrated (the RNG counter)
 };

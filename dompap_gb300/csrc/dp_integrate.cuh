@@ -87,18 +87,24 @@ __device__ __forceinline__ double dp_wrap_axis(double x, double L, int32_t& imag
 // neighbor_list_is_old (dompap/neighbor_list.py:183-201) for one particle:
 // its min-image displacement^2 since the last build against (skin/2)^2, read
 // from the fixed-point shadows in float32 and recomputed in float64 exactly
-// as the reference does only within the error bound of the threshold.
+// as the reference does only within the error bound of the threshold. With
+// `exact` (some current or reference position lies far outside the box, where
+// the shadows' periodic difference is not the reference's single-shift one)
+// always in float64.
 template <int D>
 __device__ __forceinline__ bool dp_skin_old(const void* shadow_ref, const double* pos_ref, long long n,
                                             const float* unit, const double* box, double thr, float thr_lo,
-                                            float thr_hi, long long i, const uint32_t* u, const double* x) {
+                                            float thr_hi, long long i, const uint32_t* u, const double* x,
+                                            bool exact = false) {
     typedef typename dp_shadow_t<D>::type sh_t;
-    uint32_t uref[D];
-    dp_shadow_unpack<D>(((const sh_t*)shadow_ref)[i], uref);
-    float df[D];
-    const float qf = dp_shadow_q<D>(u, uref, unit, df);
-    if (qf <= thr_lo) return false;
-    if (qf > thr_hi) return true;
+    if (!exact) {
+        uint32_t uref[D];
+        dp_shadow_unpack<D>(((const sh_t*)shadow_ref)[i], uref);
+        float df[D];
+        const float qf = dp_shadow_q<D>(u, uref, unit, df);
+        if (qf <= thr_lo) return false;
+        if (qf > thr_hi) return true;
+    }
     double d[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) d[k] = dp_min_image(x[k] - pos_ref[k * n + i], box[k]);
@@ -163,7 +169,9 @@ __device__ __forceinline__ bool dp_integrate_one(const dp_int_args& a, long long
     }
     ((typename dp_shadow_t<D>::type*)a.shadow_out)[i] = dp_shadow_pack<D>(u);
     if (WRITE64) ((typename dp_fixed64_t<D>::type*)a.pos64_out)[i] = dp_fixed64_pack<D>(X);
-    return dp_skin_old<D>(a.shadow_ref, a.pos_ref, n, a.unit, a.box, a.thr, a.thr_lo, a.thr_hi, i, u, xs);
+    // the new positions are wrapped; the list's reference positions may not be
+    return dp_skin_old<D>(a.shadow_ref, a.pos_ref, n, a.unit, a.box, a.thr, a.thr_lo, a.thr_hi, i, u, xs,
+                          a.st->ref_far != 0);
 }
 
 // Runtime dispatch over the mass mode and the integrator (uniform branches).

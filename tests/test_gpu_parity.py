@@ -164,3 +164,46 @@ def test_bad_potential_raises():
         sim.set_neighbor_list(method_str="bogus")
     with pytest.raises(ValueError):
         sim.set_pair_potential("(1-r)**2", 1.0, force_method="bogus")
+
+
+@pytest.mark.parametrize("fused", ["1", "0"])
+def test_far_positions_forces_and_steps(monkeypatch, fused):
+    """Positions left far outside the box (beyond [-L/4, 5L/4), e.g. shifted by
+    2 L): forces and the first steps follow the reference's single-shift
+    arithmetic on the raw coordinates (the float64 fallback of the
+    double-float pair loop and of the fused step); after the first step's wrap
+    the next steps run the double-float path. NVE, against the oracle's step
+    sequence (skin check -> forces -> leap-frog -> wrap)."""
+    from dompap_gb300 import Simulation
+
+    monkeypatch.setenv("DOMPAP_FUSED_STEP", fused)
+    rng = np.random.default_rng(21)
+    unit = ref.generate_positions(((0.0, 0.0, 0.0),), (4, 4, 4), (1.0, 1.0, 1.0))
+    box = np.array([4.0, 4.0, 4.0]) * (64 / 0.7 / 64.0) ** (1 / 3)
+    pos = unit * box / 4.0 + rng.normal(0, 0.03, size=unit.shape)
+    pos[3, 0] += 2 * box[0]
+    pos[17, 1] -= 3 * box[1]
+    pos[40, 2] += box[2] * 1.6
+    vel = rng.normal(0, 0.5, size=pos.shape)
+    pot, rc, skin = "4*(r**-12-r**-6)", 1.5, 0.3
+    sim = Simulation()
+    sim.box_vectors = box
+    sim.positions = pos
+    sim.velocities = vel
+    sim.betas = np.zeros_like(pos)
+    sim.image_positions = np.zeros(pos.shape, dtype=np.int32)
+    sim.masses = np.ones((64, 1))
+    sim.particle_types = np.zeros((64, 1), dtype=np.int32)
+    sim.set_pair_potential(pot, rc)
+    sim.set_neighbor_list(skin=skin, max_number_of_neighbors=64, method_str="double loop")
+    sim.set_integrator(time_step=0.002)
+    o = ref.OracleSystem(pos, vel, np.ones((64, 1)), box, pot, rc, skin, max_neighbors=64)
+    o.dt = 0.002
+    assert rel_rms(sim.get_forces(), o.forces()) <= TOL
+    for _ in range(3):
+        o.step_leap_frog()
+    sim.run_leap_frog(3)
+    assert np.max(np.abs(sim.positions - o.positions)) <= 1e-11
+    assert np.max(np.abs(sim.velocities - o.velocities)) <= 1e-10
+    assert np.array_equal(sim.image_positions, o.images)
+    assert rel_rms(sim.get_forces(), o.forces()) <= TOL
