@@ -207,3 +207,73 @@ def test_far_positions_forces_and_steps(monkeypatch, fused):
     assert np.max(np.abs(sim.velocities - o.velocities)) <= 1e-10
     assert np.array_equal(sim.image_positions, o.images)
     assert rel_rms(sim.get_forces(), o.forces()) <= TOL
+
+
+def _bare_sim(pos, box, vel=None):
+    from dompap_gb300 import Simulation
+
+    n, d = pos.shape
+    sim = Simulation()
+    sim.box_vectors = np.asarray(box, dtype=np.float64)
+    sim.positions = pos
+    sim.velocities = np.zeros((n, d)) if vel is None else vel
+    sim.betas = np.zeros((n, d))
+    sim.image_positions = np.zeros((n, d), dtype=np.int32)
+    sim.masses = np.ones((n, 1))
+    sim.particle_types = np.zeros((n, 1), dtype=np.int32)
+    return sim
+
+
+def test_single_particle_and_pair_at_cut():
+    """One particle: no pairs, zero force and energy, free flight through the
+    box with its image counter. Two particles exactly r_cut apart: the pair is
+    listed and its force is exactly zero (f(r_cut) = 0 for (1-r)^2)."""
+    sim = _bare_sim(np.array([[0.5, 0.5, 0.5]]), [3.0, 3.0, 3.0], vel=np.array([[1.0, -2.0, 0.5]]))
+    sim.set_pair_potential("(1-r)**2", 1.0)
+    sim.set_neighbor_list(skin=0.2, max_number_of_neighbors=8)
+    assert np.array_equal(sim.get_forces(), np.zeros((1, 3)))
+    assert sim.get_potential_energy() == 0.0
+    sim.set_integrator(time_step=0.05)
+    o = ref.OracleSystem(np.array([[0.5, 0.5, 0.5]]), np.array([[1.0, -2.0, 0.5]]), np.ones((1, 1)),
+                         np.array([3.0, 3.0, 3.0]), "(1-r)**2", 1.0, 0.2, max_neighbors=8)
+    o.dt = 0.05
+    for _ in range(100):  # 5 time units, through several images
+        o.step_leap_frog()
+    sim.run_leap_frog(100)
+    assert np.array_equal(sim.positions, o.positions)
+    assert np.array_equal(sim.image_positions, o.images)
+    unwrapped = sim.positions + sim.image_positions * 3.0
+    assert np.max(np.abs(unwrapped - (0.5 + 5.0 * np.array([1.0, -2.0, 0.5])))) <= 1e-12
+    sim = _bare_sim(np.array([[0.25, 0.5, 0.5], [1.25, 0.5, 0.5]]), [3.0, 3.0, 3.0])
+    sim.set_pair_potential("(1-r)**2", 1.0)
+    sim.set_neighbor_list(skin=0.2, max_number_of_neighbors=8)
+    assert np.array_equal(sim.neighbor_list, np.array([[1, -1, -1, -1, -1, -1, -1, -1],
+                                                       [0, -1, -1, -1, -1, -1, -1, -1]]))
+    assert np.array_equal(sim.get_forces(), np.zeros((2, 3)))
+
+
+def test_non_cubic_box_forces_and_steps():
+    """A strongly non-cubic box (per-axis fixed-point scales in the
+    double-float pair loop): forces and NVE steps against the oracle."""
+    rng = np.random.default_rng(31)
+    spacing = np.array([1.06, 1.13, 1.15])
+    cells = (5, 7, 4)
+    box = spacing * np.array(cells)
+    pos = ref.generate_positions(((0.0, 0.0, 0.0),), cells, tuple(spacing)) + rng.normal(0, 0.05, size=(140, 3))
+    pos -= np.floor(pos / box) * box
+    n = pos.shape[0]
+    vel = rng.normal(0, 0.3, size=(n, 3))
+    pot, rc, skin = "4*(r**-12-r**-6)", 2.0, 0.25
+    sim = _bare_sim(pos, box, vel)
+    sim.set_pair_potential(pot, rc)
+    sim.set_neighbor_list(skin=skin, max_number_of_neighbors=96, method_str="cell list")
+    sim.set_integrator(time_step=0.001)
+    o = ref.OracleSystem(pos, vel, np.ones((n, 1)), box, pot, rc, skin, max_neighbors=96)
+    o.dt = 0.001
+    assert rel_rms(sim.get_forces(), o.forces()) <= TOL
+    for _ in range(10):
+        o.step_leap_frog()
+    sim.run_leap_frog(10)
+    assert np.max(np.abs(sim.positions - o.positions)) <= 1e-11
+    assert np.array_equal(sim.image_positions, o.images)
+    assert rel_rms(sim.get_forces(), o.forces()) <= TOL
