@@ -556,6 +556,23 @@ def config_of(name):
             "l2": "working set > L2 (state + list ~ 0.2 GB for 1M particles, no flush)"}
 
 
+def reduce_over_ranks(dist, device, ms, e2e, particles, steps):
+    """Whole-job numbers over the ranks (one independent replica per rank): the
+    slowest rank's device time (max), the value as all ranks' particle-steps
+    over that time, and the e2e throughputs summed. dist is None for one rank."""
+    import torch
+
+    t = torch.tensor([ms, e2e, float(particles)], dtype=torch.float64, device=device)
+    if dist is not None:
+        mx = t[:1].clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = t[1:].clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        t = torch.cat([mx, sm])
+    ms_max, e2e_sum, n_total = (float(x) for x in t.tolist())
+    return ms_max, n_total * steps / (ms_max / 1000.0), e2e_sum
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -612,11 +629,6 @@ def main():
     from dompap_gb300 import _lib
 
     launches = int(_lib.load().dp_kernel_launches(sim._h))
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = n * args.steps * world / (ms_max / 1000.0)
     rebuilds = int(st1.rebuilds - st0.rebuilds)
     steps_per_rebuild = args.steps / max(rebuilds, 1)
 
@@ -634,9 +646,7 @@ def main():
     peak, peak_kind = measured_peaks()
     achieved = alg[dominant] * n / (kt[dominant] / 1000.0) / 1e9
     e2e_value, h2d, d2h = e2e_run(sim, args.e2e_steps)
-    e2e_total = torch.tensor([e2e_value], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        dist.all_reduce(e2e_total, op=dist.ReduceOp.SUM)
+    ms_max, value, e2e_total = reduce_over_ranks(dist, "cuda", ms, e2e_value, n, args.steps)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -645,7 +655,7 @@ def main():
         "config": dict(config_of(args.workload), parallelism=f"replicas x{world}" if world > 1 else "single system"),
         "clocks": clocks.summary(),
         "gpu_launches": launches,
-        "e2e": {"value": float(e2e_total.item()), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_total, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": PROFILED_TRAFFIC_BYTES.get((args.workload, dominant)),
