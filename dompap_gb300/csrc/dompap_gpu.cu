@@ -1579,7 +1579,11 @@ static int run_impl(dp_sim* s, long long steps, int kind, float* ms) {
         const long long c = std::min(chunk, steps - done);
         const long long step0 = s->hstat->step;  // hstat is current: every path here ends in read_status
         const long long rebuilds0 = s->hstat->rebuilds;
-        RET(backup_state(s));
+        // a chunk needs the backup only if a list build inside it can
+        // overflow: at a later step, or at its first step when a rebuild is
+        // pending (hstat is current here)
+        const bool backed_up = c > 1 || s->hstat->need_rebuild != 0;
+        if (backed_up) RET(backup_state(s));
         GraphEntry* g = nullptr;
         RET(get_graph(s, c, kind, &g));
         CK(cudaGraphLaunch(g->exec, s->stream));
@@ -1595,6 +1599,7 @@ static int run_impl(dp_sim* s, long long steps, int kind, float* ms) {
         bool grown = false;
         RET(grow_after_overflow(s, &grown));
         if (grown) {
+            if (!backed_up) return fail(DP_ERR_OVERFLOW, "neighbour list overflow without a pending build");
             if (++retries > 8) return fail(DP_ERR_OVERFLOW, "neighbour list keeps overflowing");
             RET(restore_state(s));
             s->hstat->step = step0;
@@ -1727,30 +1732,60 @@ int dp_set_precision(dp_sim* s, int precision) {
 }
 
 // --------------------------- state ----------------------------------------
-static int upload_aos_f64(dp_sim* s, const double* host, double* dev_soa) {
+// The device's view of a page-locked host array (cudaHostAlloc / registered),
+// or nullptr for pageable memory. The transposing kernels then read or write
+// the host array directly over the host link: one pass, no staging copy.
+static const void* mapped_view(const void* host) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
+}
+
+// host AoS (n, dim) -> device SoA; the caller synchronises (the host array
+// must not change before that).
+static int upload_aos_f64_async(dp_sim* s, const double* host, double* dev_soa) {
     if (!host) return fail(DP_ERR_ARG, "null array");
-    const size_t bytes = (size_t)s->n * s->dim * sizeof(double);
-    // stage through the force buffer's twin (bk_pos) to transpose on the device
-    CK(cudaMemcpyAsync(s->bk_pos, host, bytes, cudaMemcpyHostToDevice, s->stream));
-    k_aos_to_soa_f64<<<grid_for(s->n * s->dim, kBlock), kBlock, 0, s->stream>>>(s->bk_pos, dev_soa, s->n, s->dim);
+    const unsigned g = grid_for(s->n * s->dim, kBlock);
+    if (const double* view = (const double*)mapped_view(host)) {
+        k_aos_to_soa_f64<<<g, kBlock, 0, s->stream>>>(view, dev_soa, s->n, s->dim);
+    } else {
+        // stage through the backup buffer to transpose on the device
+        CK(cudaMemcpyAsync(s->bk_pos, host, (size_t)s->n * s->dim * sizeof(double), cudaMemcpyHostToDevice,
+                           s->stream));
+        k_aos_to_soa_f64<<<g, kBlock, 0, s->stream>>>(s->bk_pos, dev_soa, s->n, s->dim);
+    }
     CK(cudaGetLastError());
+    return DP_OK;
+}
+
+static int upload_aos_f64(dp_sim* s, const double* host, double* dev_soa) {
+    RET(upload_aos_f64_async(s, host, dev_soa));
     CK(cudaStreamSynchronize(s->stream));
     return DP_OK;
 }
 
 static int download_aos_f64(dp_sim* s, const double* dev_soa, double* host) {
     if (!host) return fail(DP_ERR_ARG, "null array");
-    const size_t bytes = (size_t)s->n * s->dim * sizeof(double);
-    k_soa_to_aos_f64<<<grid_for(s->n * s->dim, kBlock), kBlock, 0, s->stream>>>(dev_soa, s->bk_vel, s->n, s->dim);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(host, s->bk_vel, bytes, cudaMemcpyDeviceToHost, s->stream));
+    const unsigned g = grid_for(s->n * s->dim, kBlock);
+    if (double* view = (double*)mapped_view(host)) {
+        k_soa_to_aos_f64<<<g, kBlock, 0, s->stream>>>(dev_soa, view, s->n, s->dim);
+        CK(cudaGetLastError());
+    } else {
+        k_soa_to_aos_f64<<<g, kBlock, 0, s->stream>>>(dev_soa, s->bk_vel, s->n, s->dim);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(host, s->bk_vel, (size_t)s->n * s->dim * sizeof(double), cudaMemcpyDeviceToHost,
+                           s->stream));
+    }
     CK(cudaStreamSynchronize(s->stream));
     return DP_OK;
 }
 
 int dp_set_positions(dp_sim* s, const double* p) {
     if (!s) return fail(DP_ERR_ARG, "null handle");
-    RET(upload_aos_f64(s, p, s->pos));
+    RET(upload_aos_f64_async(s, p, s->pos));
     if (s->have_box) RET(launch_shadow(s));
     CK(cudaStreamSynchronize(s->stream));
     return DP_OK;
