@@ -289,6 +289,7 @@ struct NlArgs {
     double cutoff;
     float lo2;  // float32 r^2 below this: certainly inside the cutoff
     float hi2;  // float32 r^2 above this: certainly outside
+    int half;   // 1: partners j > i only (the surrogate mode's kernels use each pair once)
 };
 
 template <int D>
@@ -328,7 +329,7 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_cells(NlArgs a) {
         const int32_t* mem = a.cell_mem + l * a.ccap;
         for (int t = 0; t < m; ++t) {
             const int j = mem[t];
-            if (j == i) continue;
+            if (a.half ? j <= i : j == i) continue;
             // float32 pre-test on the fixed-point displacement (nearest image,
             // never longer than the single-shift one); float64 only near the cutoff
             uint32_t uj[D];
@@ -378,7 +379,7 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_allpairs(NlArgs a) {
             const int lim = (int)min((long long)kBlock, n - base);
             for (int t = 0; t < lim; ++t) {
                 const long long j = base + t;
-                if (j == i) continue;
+                if (a.half ? j <= i : j == i) continue;
                 double d[D];
 #pragma unroll
                 for (int k = 0; k < D; ++k) d[k] = dp_min_image(xi[k] - tile[k][t], a.box[k]);
@@ -452,6 +453,34 @@ __global__ void k_nl_export(const int32_t* __restrict__ nl, const int32_t* __res
         row[u + 1] = v;
     }
     for (int k = m; k < kout; ++k) row[k] = -1;
+}
+
+// A half list (partners j > i only) closed into the full one: row i gets its
+// own entries and i from every row j < i that holds it. The distance test is
+// symmetric (the min-image displacement of j - i is the negated one of i - j
+// and the sum of squares is the same), so the closure is the list a full
+// build at the same reference positions makes. Count pass, then scatter into
+// an unsorted column-major list that k_nl_export sorts.
+__global__ void k_nl_half_count(const int32_t* __restrict__ nl, const int32_t* __restrict__ cnt, int32_t* fcnt,
+                                int32_t* fmax, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = cnt[i];
+    for (int k = 0; k < c; ++k) atomicAdd(fcnt + nl[(long long)k * n + i], 1);
+    const int mine = atomicAdd(fcnt + i, c) + c;
+    atomicMax(fmax, mine);
+}
+
+__global__ void k_nl_half_scatter(const int32_t* __restrict__ nl, const int32_t* __restrict__ cnt, int32_t* fill,
+                                  int32_t* full, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = cnt[i];
+    for (int k = 0; k < c; ++k) {
+        const int32_t j = nl[(long long)k * n + i];
+        full[(long long)atomicAdd(fill + i, 1) * n + i] = j;
+        full[(long long)atomicAdd(fill + j, 1) * n + j] = (int32_t)i;
+    }
 }
 
 // --------------------------- integrators ----------------------------------
@@ -764,6 +793,9 @@ struct dp_sim {
     // fill the GPU; on par with mma.sync there), mma.sync below; 1 = tcgen05;
     // 2 = mma.sync (DOMPAP_MLP_TENSOR=tcgen05 | mma)
     int mlp_tensor = 0;
+    // neighbour lists hold partners j > i only in the surrogate mode (its
+    // kernels use each pair once); an export builds a full one for the moment
+    bool nl_half = false;         // kind of the list currently built
     // second set of position buffers: a fused step reads pos/shadow/pos64 and
     // writes these, then the two sets change roles
     double* pos_alt = nullptr;
@@ -1017,9 +1049,13 @@ static void fill_cell_args(const dp_sim* s, CellArgs& a) {
 }
 
 // The gated rebuild sequence (no effect unless need_rebuild is set).
+// The surrogate mode uses each pair once: its lists hold the partners j > i only.
+static bool list_half(const dp_sim* s) { return s->precision == DP_PREC_MLP; }
+
 static int launch_rebuild(dp_sim* s, long long* launches) {
     const unsigned gp = grid_for(s->n, kBlock);
     NlArgs na{};
+    na.half = list_half(s) ? 1 : 0;
     na.pos = s->pos;
     na.pos_ref = s->pos_ref;
     na.shadow = s->shadow;
@@ -1341,7 +1377,7 @@ static int update_nl(dp_sim* s, bool check, int* rebuilt) {
     RET(configure_nl(s));
     RET(read_status(s));
     const long long before = s->hstat->rebuilds;
-    if (!s->nl_built || !check) {
+    if (!s->nl_built || !check || s->nl_half != list_half(s)) {
         s->hstat->need_rebuild = 1;
         RET(write_status(s));
     } else {
@@ -1363,6 +1399,7 @@ static int update_nl(dp_sim* s, bool check, int* rebuilt) {
         RET(write_status(s));
     }
     s->nl_built = true;
+    s->nl_half = list_half(s);
     if (rebuilt) *rebuilt = (s->hstat->rebuilds != before) ? 1 : 0;
     return DP_OK;
 }
@@ -2046,16 +2083,48 @@ int dp_get_neighbor_list(dp_sim* s, int32_t* out, int kmax, int32_t* max_count) 
     RET(require_ready(s));
     if (!out || kmax < 1) return fail(DP_ERR_ARG, "bad output");
     RET(update_nl(s, true, nullptr));
+    const unsigned g = grid_for(s->n, kBlock);
+    const int32_t* rows = s->nl;
+    const int32_t* counts = s->cnt;
+    int32_t* full = nullptr;  // half lists: the full list, unsorted, column-major
+    int32_t* fcnt = nullptr;  // its counts (n) and their maximum
+    int32_t fmax = s->hstat->max_neighbors;
+    cudaError_t e = cudaSuccess;
+    if (s->nl_half) {
+        // the reference's list is the full one (every partner of every particle)
+        RET(dalloc_t(&fcnt, (size_t)s->n + 1));
+        e = cudaMemsetAsync(fcnt, 0, ((size_t)s->n + 1) * sizeof(int32_t), s->stream);
+        if (e == cudaSuccess) {
+            k_nl_half_count<<<g, kBlock, 0, s->stream>>>(s->nl, s->cnt, fcnt, fcnt + s->n, s->n);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&fmax, fcnt + s->n, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e == cudaSuccess && dalloc_t(&full, (size_t)s->n * std::max(fmax, 1)) != DP_OK)
+            e = cudaErrorMemoryAllocation;
+        if (e == cudaSuccess) e = cudaMemsetAsync(fcnt, 0, (size_t)s->n * sizeof(int32_t), s->stream);
+        if (e == cudaSuccess) {
+            k_nl_half_scatter<<<g, kBlock, 0, s->stream>>>(s->nl, s->cnt, fcnt, full, s->n);
+            e = cudaGetLastError();
+        }
+        rows = full;
+        counts = fcnt;
+    }
     int32_t* dout = nullptr;
-    RET(dalloc_t(&dout, (size_t)s->n * kmax));
-    k_nl_export<<<grid_for(s->n, kBlock), kBlock, 0, s->stream>>>(s->nl, s->cnt, dout, s->n, kmax);
-    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && dalloc_t(&dout, (size_t)s->n * kmax) != DP_OK) e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) {
+        k_nl_export<<<g, kBlock, 0, s->stream>>>(rows, counts, dout, s->n, kmax);
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(out, dout, (size_t)s->n * kmax * sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     cudaFree(dout);
+    cudaFree(full);
+    cudaFree(fcnt);
     if (e != cudaSuccess) return fail(DP_ERR_CUDA, std::string("neighbour-list export: ") + cudaGetErrorString(e));
-    if (max_count) *max_count = s->hstat->max_neighbors;
+    if (max_count) *max_count = fmax;
     return DP_OK;
 }
 

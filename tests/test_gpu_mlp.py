@@ -119,6 +119,26 @@ def test_surrogate_forces_deterministic_and_balanced(surrogate):
     assert np.max(np.abs(f1)) > 1.0
 
 
+def test_surrogate_mode_half_lists_export_full(surrogate):
+    """The surrogate mode keeps neighbour lists of partners j > i only (its
+    kernels use each pair once); the export closes them into the reference's
+    full list at the list's reference positions, without a rebuild, and forces
+    do not change across the export."""
+    from oracle import numpy_ref as ref
+
+    sim = _liquid(seed=4)
+    sim.set_pair_surrogate(surrogate)
+    f1 = sim.get_forces()
+    updates = sim.number_of_neighbor_list_updates
+    exported = np.array(sim.neighbor_list)
+    assert sim.number_of_neighbor_list_updates == updates
+    want, _ = ref.neighbor_list_double_loop(np.array(sim.positions_neighbour_list), np.array(sim.box_vectors),
+                                            3.0 + 0.3, exported.shape[1])
+    assert np.array_equal(exported, want)
+    f2 = sim.get_forces()
+    assert np.array_equal(f1, f2)
+
+
 def test_tcgen05_pass_matches_mma_sync_pass(surrogate, monkeypatch):
     """The surrogate's 128 x 64 x 64 layer on the fifth-generation tensor
     cores (tcgen05.mma, TMEM accumulator) and on mma.sync give the same
