@@ -124,163 +124,181 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
     for (int k = 0; k < D; ++k) xi[k] = a.pos[k * n + i];
 #endif
 #endif
+    // Two passes over windows of up to 32 listed neighbours. Pass 1 runs the
+    // float32 pre-filter on the shadows and keeps a bit per neighbour that
+    // may lie within r_cut * sigma_max; pass 2 evaluates the pair terms of
+    // the kept ones only, in list order. A warp then runs the pair arithmetic
+    // as often as its busiest lane has kept neighbours, not once per listed
+    // one (in a dense liquid with a thin skin most listed neighbours of most
+    // lanes are outside r_cut at any step).
     const int c = a.cnt[i];
     const int32_t* __restrict__ row = a.nl + i;
-    for (int kk = 0; kk < c; ++kk) {
-        const int j = __ldg(row + (long long)kk * n);
-        // the virial is the reference's upper-triangle sum over n < m with
-        // sigma(n, m), epsilon(n, m) (dompap/potential.py:265-278)
-        if (ACC == DP_ACC_VIRIAL && j <= i) continue;
-        uint32_t uj[D];
-#if DP_FF
-        // one gather per neighbour: the 64-bit fixed point, whose upper words
-        // are the shadow
-        unsigned long long Xj[D];
-        if (ff_ok) {
-            dp_fixed64_unpack<D>(p64[j], Xj);
-#pragma unroll
-            for (int k = 0; k < D; ++k) uj[k] = (uint32_t)(Xj[k] >> 32);
-        } else {
+    for (int base = 0; base < c; base += 32) {
+        const int w = min(32, c - base);
+        uint32_t kept = 0;
+#pragma unroll 4
+        for (int t = 0; t < w; ++t) {
+            const int j = __ldg(row + (long long)(base + t) * n);
+            // the virial is the reference's upper-triangle sum over n < m with
+            // sigma(n, m), epsilon(n, m) (dompap/potential.py:265-278)
+            if (ACC == DP_ACC_VIRIAL && j <= i) continue;
+            uint32_t uj[D];
             dp_shadow_unpack<D>(__ldg(sh + j), uj);
+            float df[D];
+            if (dp_shadow_q<D>(ui, uj, a.unit, df) <= a.cut2f) kept |= 1u << t;
         }
-#else
-        dp_shadow_unpack<D>(__ldg(sh + j), uj);
-#endif
-        float df[D];
-        const float qf = dp_shadow_q<D>(ui, uj, a.unit, df);
-        if (qf > a.cut2f) continue;  // certainly beyond r_cut * sigma_max
-#if DP_REAL_IS_FLOAT
-        double sig, isig, eps;
-        dp_pair_params(a, i, ti, j, sig, isig, eps);
-        // FP32 pair arithmetic on the fixed-point displacement.
-        const float rinv = rsqrtf(qf);
-        const float r = qf * rinv;
-#if DP_SIGMA_ONE
-        const float s = r, sinv = rinv;
-#else
-        const float s = r * (float)isig, sinv = rinv * (float)sig;
-#endif
-        if (s > (float)a.rcut) continue;
-        const float e = (float)eps;
-        if (ACC == DP_ACC_FORCE) {
-#if DP_EPS_ONE
-            const float sf = dp_pair_f<float>(s, sinv);
-#else
-            const float sf = e * dp_pair_f<float>(s, sinv);
-#endif
-            const float g = sf * rinv;
-#pragma unroll
-            for (int k = 0; k < D; ++k) acc_v[k] = fmaf(g, df[k], acc_v[k]);
-        } else if (ACC == DP_ACC_ENERGY) {
-            acc_s += (double)(e * dp_pair_u<float>(s, sinv));
-        } else if (ACC == DP_ACC_VIRIAL) {
-            acc_s += (double)(e * dp_pair_f<float>(s, sinv) * r);
-        } else {
-            acc_s += (double)(e * dp_pair_c<float>(s, sinv) + (float)(D - 1) * (-e * dp_pair_f<float>(s, sinv)) * rinv);
-        }
-#else
+        while (kept) {
+            const int t = __ffs(kept) - 1;
+            kept &= kept - 1;
+            const int j = __ldg(row + (long long)(base + t) * n);
+            uint32_t uj[D];
 #if DP_FF
-        if (ff_ok) {
-            // double-float pair arithmetic on the exact fixed-point displacement
-            dpff d[D];
+            unsigned long long Xj[D];
+            if (ff_ok) {
+                dp_fixed64_unpack<D>(p64[j], Xj);
 #pragma unroll
-            for (int k = 0; k < D; ++k) d[k] = dpff_from_ll((long long)(Xi[k] - Xj[k])) * U[k];
-            dpff q = dpff_sqr_unnormalised(d[0]);
-#pragma unroll
-            for (int k = 1; k < D; ++k) dpff_accumulate(q, dpff_sqr_unnormalised(d[k]));
-            q = dpff_quick_two_sum(q.hi, q.lo);
-            const dpff rinv = dpff_rsqrt(q);
-            const dpff r = q * rinv;
-#if DP_PMODE == 0
-            const dpff fsig = sig_c, fisig = isig_c, feps = eps_c;
-#elif DP_PMODE == 1
-            const int tj = __ldg(a.types + j);
-            const float2* tri = a.ff_tab + 3 * (ti * a.ntypes + tj);
-            const float2 t0 = __ldg(tri), t1 = __ldg(tri + 1), t2 = __ldg(tri + 2);
-            const dpff fsig(t0.x, t0.y), fisig(t1.x, t1.y), feps(t2.x, t2.y);
+                for (int k = 0; k < D; ++k) uj[k] = (uint32_t)(Xj[k] >> 32);
+            } else {
+                dp_shadow_unpack<D>(__ldg(sh + j), uj);
+            }
 #else
+            dp_shadow_unpack<D>(__ldg(sh + j), uj);
+#endif
+            float df[D];
+            const float qf = dp_shadow_q<D>(ui, uj, a.unit, df);
+#if DP_REAL_IS_FLOAT
             double sig, isig, eps;
             dp_pair_params(a, i, ti, j, sig, isig, eps);
-            const dpff fsig(sig), fisig(isig), feps(eps);
-#endif
+            // FP32 pair arithmetic on the fixed-point displacement.
+            const float rinv = rsqrtf(qf);
+            const float r = qf * rinv;
 #if DP_SIGMA_ONE
-            const dpff s = r, sinv = rinv;
+            const float s = r, sinv = rinv;
 #else
-            const dpff s = r * fisig, sinv = rinv * fsig;
+            const float s = r * (float)isig, sinv = rinv * (float)sig;
 #endif
-            if (!(rcut_finite && fabsf(s.hi - rcut_f) <= 1e-5f * rcut_f)) {
-                if (s.hi > rcut_f) continue;
-                if (ACC == DP_ACC_FORCE) {
+            if (s > (float)a.rcut) continue;
+            const float e = (float)eps;
+            if (ACC == DP_ACC_FORCE) {
 #if DP_EPS_ONE
-                    const dpff g = dp_pair_f<dpff>(s, sinv) * rinv;
+                const float sf = dp_pair_f<float>(s, sinv);
 #else
-                    const dpff g = feps * dp_pair_f<dpff>(s, sinv) * rinv;
+                const float sf = e * dp_pair_f<float>(s, sinv);
 #endif
+                const float g = sf * rinv;
 #pragma unroll
-                    for (int k = 0; k < D; ++k) dpff_accumulate_prod(facc[k], g, d[k]);
-                } else if (ACC == DP_ACC_ENERGY) {
-                    dpff_accumulate(sacc, feps * dp_pair_u<dpff>(s, sinv));
-                } else if (ACC == DP_ACC_VIRIAL) {
-                    dpff_accumulate(sacc, feps * dp_pair_f<dpff>(s, sinv) * r);
-                } else {
-                    const dpff sf = feps * dp_pair_f<dpff>(s, sinv);
-                    dpff_accumulate(sacc, feps * dp_pair_c<dpff>(s, sinv) - dpff(D - 1) * sf * rinv);
-                }
-                continue;
+                for (int k = 0; k < D; ++k) acc_v[k] = fmaf(g, df[k], acc_v[k]);
+            } else if (ACC == DP_ACC_ENERGY) {
+                acc_s += (double)(e * dp_pair_u<float>(s, sinv));
+            } else if (ACC == DP_ACC_VIRIAL) {
+                acc_s += (double)(e * dp_pair_f<float>(s, sinv) * r);
+            } else {
+                acc_s += (double)(e * dp_pair_c<float>(s, sinv) + (float)(D - 1) * (-e * dp_pair_f<float>(s, sinv)) * rinv);
             }
-            // within float rounding of r_cut: the float64 path below
-#pragma unroll
-            for (int k = 0; k < D; ++k) xi[k] = a.pos[k * n + i];
-        }
-        used64 = true;
-#endif
-        // FP64 pair arithmetic. d and r^2 follow the reference exactly; 1/r
-        // comes from one reciprocal square root (no divisions), and where s
-        // lies within a few ulp of r_cut, r = sqrt(r^2) and s = r / sigma are
-        // recomputed with IEEE operations so the cut decision is the
-        // reference's.
-        double sig, isig, eps;
-        dp_pair_params(a, i, ti, j, sig, isig, eps);
-        double d[D];
-#pragma unroll
-        for (int k = 0; k < D; ++k) d[k] = dp_min_image(xi[k] - __ldg(a.pos + k * n + j), a.box[k]);
-        const double q = dp_sqsum_exact<D>(d);
-        const double rinv = rsqrt(q);
-        double r = q * rinv;
-#if DP_SIGMA_ONE
-        double s = r;
-        const double sinv = rinv;
 #else
-        double s = r * isig;
-        const double sinv = rinv * sig;
-#endif
-        if (fabs(s - a.rcut) <= 1e-14 * a.rcut) {
-            r = sqrt(q);
-#if DP_SIGMA_ONE
-            s = r;
+#if DP_FF
+            if (ff_ok) {
+                // double-float pair arithmetic on the exact fixed-point displacement
+                dpff d[D];
+#pragma unroll
+                for (int k = 0; k < D; ++k) d[k] = dpff_from_ll((long long)(Xi[k] - Xj[k])) * U[k];
+                dpff q = dpff_sqr_unnormalised(d[0]);
+#pragma unroll
+                for (int k = 1; k < D; ++k) dpff_accumulate(q, dpff_sqr_unnormalised(d[k]));
+                q = dpff_quick_two_sum(q.hi, q.lo);
+                const dpff rinv = dpff_rsqrt(q);
+                const dpff r = q * rinv;
+#if DP_PMODE == 0
+                const dpff fsig = sig_c, fisig = isig_c, feps = eps_c;
+#elif DP_PMODE == 1
+                const int tj = __ldg(a.types + j);
+                const float2* tri = a.ff_tab + 3 * (ti * a.ntypes + tj);
+                const float2 t0 = __ldg(tri), t1 = __ldg(tri + 1), t2 = __ldg(tri + 2);
+                const dpff fsig(t0.x, t0.y), fisig(t1.x, t1.y), feps(t2.x, t2.y);
 #else
-            s = r / sig;
+                double sig, isig, eps;
+                dp_pair_params(a, i, ti, j, sig, isig, eps);
+                const dpff fsig(sig), fisig(isig), feps(eps);
 #endif
-        }
-        if (s > a.rcut) continue;
-        if (ACC == DP_ACC_FORCE) {
+#if DP_SIGMA_ONE
+                const dpff s = r, sinv = rinv;
+#else
+                const dpff s = r * fisig, sinv = rinv * fsig;
+#endif
+                if (!(rcut_finite && fabsf(s.hi - rcut_f) <= 1e-5f * rcut_f)) {
+                    if (s.hi > rcut_f) continue;
+                    if (ACC == DP_ACC_FORCE) {
 #if DP_EPS_ONE
-            const double sf = dp_pair_f<double>(s, sinv);
+                        const dpff g = dp_pair_f<dpff>(s, sinv) * rinv;
 #else
-            const double sf = eps * dp_pair_f<double>(s, sinv);
+                        const dpff g = feps * dp_pair_f<dpff>(s, sinv) * rinv;
 #endif
-            const double g = sf * rinv;
 #pragma unroll
-            for (int k = 0; k < D; ++k) acc_v[k] = fma(g, d[k], acc_v[k]);
-        } else if (ACC == DP_ACC_ENERGY) {
-            acc_s += eps * dp_pair_u<double>(s, sinv);
-        } else if (ACC == DP_ACC_VIRIAL) {
-            acc_s += eps * dp_pair_f<double>(s, sinv) * r;
-        } else {
-            const double sf = eps * dp_pair_f<double>(s, sinv);
-            acc_s += eps * dp_pair_c<double>(s, sinv) + (double)(D - 1) * (-sf) * rinv;
-        }
+                        for (int k = 0; k < D; ++k) dpff_accumulate_prod(facc[k], g, d[k]);
+                    } else if (ACC == DP_ACC_ENERGY) {
+                        dpff_accumulate(sacc, feps * dp_pair_u<dpff>(s, sinv));
+                    } else if (ACC == DP_ACC_VIRIAL) {
+                        dpff_accumulate(sacc, feps * dp_pair_f<dpff>(s, sinv) * r);
+                    } else {
+                        const dpff sf = feps * dp_pair_f<dpff>(s, sinv);
+                        dpff_accumulate(sacc, feps * dp_pair_c<dpff>(s, sinv) - dpff(D - 1) * sf * rinv);
+                    }
+                    continue;
+                }
+                // within float rounding of r_cut: the float64 path below
+#pragma unroll
+                for (int k = 0; k < D; ++k) xi[k] = a.pos[k * n + i];
+            }
+            used64 = true;
 #endif
+            // FP64 pair arithmetic. d and r^2 follow the reference exactly; 1/r
+            // comes from one reciprocal square root (no divisions), and where s
+            // lies within a few ulp of r_cut, r = sqrt(r^2) and s = r / sigma are
+            // recomputed with IEEE operations so the cut decision is the
+            // reference's.
+            double sig, isig, eps;
+            dp_pair_params(a, i, ti, j, sig, isig, eps);
+            double d[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) d[k] = dp_min_image(xi[k] - __ldg(a.pos + k * n + j), a.box[k]);
+            const double q = dp_sqsum_exact<D>(d);
+            const double rinv = rsqrt(q);
+            double r = q * rinv;
+#if DP_SIGMA_ONE
+            double s = r;
+            const double sinv = rinv;
+#else
+            double s = r * isig;
+            const double sinv = rinv * sig;
+#endif
+            if (fabs(s - a.rcut) <= 1e-14 * a.rcut) {
+                r = sqrt(q);
+#if DP_SIGMA_ONE
+                s = r;
+#else
+                s = r / sig;
+#endif
+            }
+            if (s > a.rcut) continue;
+            if (ACC == DP_ACC_FORCE) {
+#if DP_EPS_ONE
+                const double sf = dp_pair_f<double>(s, sinv);
+#else
+                const double sf = eps * dp_pair_f<double>(s, sinv);
+#endif
+                const double g = sf * rinv;
+#pragma unroll
+                for (int k = 0; k < D; ++k) acc_v[k] = fma(g, d[k], acc_v[k]);
+            } else if (ACC == DP_ACC_ENERGY) {
+                acc_s += eps * dp_pair_u<double>(s, sinv);
+            } else if (ACC == DP_ACC_VIRIAL) {
+                acc_s += eps * dp_pair_f<double>(s, sinv) * r;
+            } else {
+                const double sf = eps * dp_pair_f<double>(s, sinv);
+                acc_s += eps * dp_pair_c<double>(s, sinv) + (double)(D - 1) * (-sf) * rinv;
+            }
+#endif
+        }
     }
 #if DP_FF
     // double-float -> float64 by moving bits (one float64 add per value)
