@@ -133,6 +133,8 @@ _SIGNATURES = {
     "dp_batch_set_neighbor_list": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_int]),
     "dp_nvrtc_check": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
                                       ctypes.POINTER(ctypes.c_int64)]),
+    "dp_nvrtc_resources": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
+                                          ctypes.c_char_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
     "dp_batch_list_stats": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                            ctypes.POINTER(ctypes.c_int32)]),
     "dp_batch_observables": (ctypes.c_int, [_P, _D, ctypes.c_int]),

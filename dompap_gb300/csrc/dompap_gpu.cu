@@ -707,13 +707,16 @@ static std::mutex g_lib_mutex;
 static std::unordered_map<std::string, PairLib> g_libs;
 
 // NVRTC: program text -> sm_103a CUBIN (host only; no GPU needed).
-static int nvrtc_cubin(const std::string& src, std::vector<char>* cubin) {
+// resource_log (optional): compile with the assembler's verbose report
+// (registers, spill bytes, shared memory per kernel) and return that log.
+static int nvrtc_cubin(const std::string& src, std::vector<char>* cubin, std::string* resource_log = nullptr) {
     nvrtcProgram prog;
     nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "dompap_pair.cu", 0, nullptr, nullptr);
     if (r != NVRTC_SUCCESS) return fail(DP_ERR_NVRTC, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
     const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--fmad=true",
-                          "-DDP_NVRTC=1"};
-    r = nvrtcCompileProgram(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+                          "-DDP_NVRTC=1", "--ptxas-options=-v"};
+    const int nopt = (int)(sizeof(opts) / sizeof(opts[0])) - (resource_log ? 0 : 1);
+    r = nvrtcCompileProgram(prog, nopt, opts);
     if (r != NVRTC_SUCCESS) {
         size_t log_size = 0;
         nvrtcGetProgramLogSize(prog, &log_size);
@@ -721,6 +724,12 @@ static int nvrtc_cubin(const std::string& src, std::vector<char>* cubin) {
         if (log_size) nvrtcGetProgramLog(prog, &log[0]);
         nvrtcDestroyProgram(&prog);
         return fail(DP_ERR_NVRTC, std::string("NVRTC compile of the pair potential failed: ") + log);
+    }
+    if (resource_log) {
+        size_t log_size = 0;
+        nvrtcGetProgramLogSize(prog, &log_size);
+        resource_log->assign(log_size, '\0');
+        if (log_size) nvrtcGetProgramLog(prog, &(*resource_log)[0]);
     }
     size_t cubin_size = 0;
     nvrtcGetCUBINSize(prog, &cubin_size);
@@ -817,6 +826,7 @@ struct dp_sim {
     std::vector<double> class_mass{1.0};
     uint8_t* mclass = nullptr;
     double* mcoef = nullptr;      // [nclass][5]
+    float2* mcoef_f = nullptr;    // [nclass]: float32 b/(2m), sqrt(2 alpha T dt)
     double* class_mass_dev = nullptr;
     double* mass = nullptr;       // per particle (mode 2)
 
@@ -976,6 +986,10 @@ static int upload_mass_coefficients(dp_sim* s) {
     }
     RET(dalloc_t(&s->mcoef, coef.size()));
     CK(cudaMemcpy(s->mcoef, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<float2> coef_f((size_t)nclass);
+    for (int c = 0; c < nclass; ++c) coef_f[c] = make_float2((float)coef[c * 5 + 2], (float)coef[c * 5 + 3]);
+    RET(dalloc_t(&s->mcoef_f, coef_f.size()));
+    CK(cudaMemcpy(s->mcoef_f, coef_f.data(), coef_f.size() * sizeof(float2), cudaMemcpyHostToDevice));
     RET(dalloc_t(&s->class_mass_dev, (size_t)nclass));
     CK(cudaMemcpy(s->class_mass_dev, s->class_mass.data(), nclass * sizeof(double), cudaMemcpyHostToDevice));
     s->version++;
@@ -1228,6 +1242,7 @@ static void fill_int_args(const dp_sim* s, dp_int_args& a, long long step_offset
     a.shadow_ref = s->shadow_ref;
     a.mclass = s->mclass;
     a.mcoef = s->mcoef;
+    a.mcoef_f = s->mcoef_f;
     a.mass = s->mass;
     a.st = s->dstat;
     a.n = s->n;
@@ -1250,6 +1265,8 @@ static void fill_int_args(const dp_sim* s, dp_int_args& a, long long step_offset
         a.coef[2] = b / 2 / m;
         a.coef[3] = std::sqrt(beta_variance);
         a.coef[4] = s->dt / m;
+        a.coef_f[0] = (float)a.coef[2];
+        a.coef_f[1] = (float)a.coef[3];
     }
     a.temperature = s->temperature;
     a.tau = s->tau;
@@ -1737,7 +1754,7 @@ int dp_destroy(dp_sim* s) {
     void* bufs[] = {s->pos, s->vel, s->beta, s->force, s->pos_ref, s->img, s->shadow, s->shadow_ref, s->pos64,
                     s->pos_alt, s->shadow_alt, s->pos64_alt, s->mlp_fx,
                     s->ff_tab, s->bk_pos,
-                    s->bk_vel, s->bk_beta, s->bk_img, s->mclass, s->mcoef, s->class_mass_dev, s->mass, s->types,
+                    s->bk_vel, s->bk_beta, s->bk_img, s->mclass, s->mcoef, s->mcoef_f, s->class_mass_dev, s->mass, s->types,
                     s->sig_tab, s->eps_tab, s->isig_tab, s->nl, s->cnt, s->cell_cnt, s->cell_mem, s->dstat,
                     s->partial, s->dsum};
     for (void* b : bufs)
@@ -1983,10 +2000,15 @@ static std::string pair_program(int dim, int precision, int pmode, bool sig_one,
 // 4, 5, 7 and 8). With per-type or per-pair tables the pair loop spills
 // ~600 bytes under that cap (the Wahnstrom mixture ran 17 % slower), so those
 // use 4 (64 registers).
+static int step_blocks_for(int dim, int pmode) {
+    (void)dim;
+    return pmode == DP_PAIR_CONST ? 6 : 4;
+}
+
 static int rebuild_pair_lib(dp_sim* s) {
     const bool sig_one = s->pmode == DP_PAIR_CONST && s->sigma == 1.0;
     const bool eps_one = s->pmode == DP_PAIR_CONST && s->epsilon == 1.0;
-    const int step_blocks = s->pmode == DP_PAIR_CONST ? 6 : 4;
+    const int step_blocks = step_blocks_for(s->dim, s->pmode);
     const std::string src =
         pair_program(s->dim, s->precision, s->pmode, sig_one, eps_one, s->pot_src, false, step_blocks);
     PairLib pl;
@@ -2927,18 +2949,37 @@ int dp_batch_run(dp_batch* b, int64_t steps, int sample_every, int nve, int reco
     return DP_OK;
 }
 
-int dp_nvrtc_check(int dim, int precision, int pair_mode, int with_batch, const char* device_source,
-                   int64_t* cubin_bytes) {
+static int nvrtc_check_impl(int dim, int precision, int pair_mode, int with_batch, const char* device_source,
+                            int64_t* cubin_bytes, std::string* resource_log) {
     if (!device_source) return fail(DP_ERR_ARG, "null source");
     if (dim < 2 || dim > 4) return fail(DP_ERR_ARG, "dimension must be 2, 3 or 4");
     if (precision != DP_PREC_FP64 && precision != DP_PREC_FP32 && precision != DP_PREC_MLP)
         return fail(DP_ERR_ARG, "unknown precision");
     if (pair_mode < DP_PAIR_CONST || pair_mode > DP_PAIR_DENSE) return fail(DP_ERR_ARG, "unknown pair mode");
     const bool one = pair_mode == DP_PAIR_CONST;
-    const std::string src = pair_program(dim, precision, pair_mode, one, one, device_source, with_batch != 0);
+    const std::string src = pair_program(dim, precision, pair_mode, one, one, device_source, with_batch != 0,
+                                         step_blocks_for(dim, pair_mode));
     std::vector<char> cubin;
-    RET(nvrtc_cubin(src, &cubin));
+    RET(nvrtc_cubin(src, &cubin, resource_log));
     if (cubin_bytes) *cubin_bytes = (int64_t)cubin.size();
+    return DP_OK;
+}
+
+int dp_nvrtc_check(int dim, int precision, int pair_mode, int with_batch, const char* device_source,
+                   int64_t* cubin_bytes) {
+    return nvrtc_check_impl(dim, precision, pair_mode, with_batch, device_source, cubin_bytes, nullptr);
+}
+
+int dp_nvrtc_resources(int dim, int precision, int pair_mode, int with_batch, const char* device_source, char* log,
+                       int64_t log_capacity, int64_t* log_bytes) {
+    if (!log || log_capacity < 1) return fail(DP_ERR_ARG, "bad log buffer");
+    std::string text;
+    RET(nvrtc_check_impl(dim, precision, pair_mode, with_batch, device_source, nullptr, &text));
+    const size_t len = strnlen(text.c_str(), text.size());
+    const size_t k = std::min(len, (size_t)(log_capacity - 1));
+    memcpy(log, text.data(), k);
+    log[k] = '\0';
+    if (log_bytes) *log_bytes = (int64_t)len;
     return DP_OK;
 }
 

@@ -224,6 +224,18 @@ __device__ __forceinline__ double dp_f2d(float z) {
     return __longlong_as_double((long long)(sign | (ed << 52) | mant));
 }
 
+// float64 -> float32 by moving bits, truncating the mantissa (exact for a
+// float64 that holds a float32 value; values beyond float32 range become
+// infinities, below it zero). No float64 instruction.
+__device__ __forceinline__ float dp_d2f_trunc(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FFu) - 1023 + 127;
+    const uint32_t sign = (uint32_t)(b >> 63) << 31;
+    const uint32_t mant = (uint32_t)((b >> 29) & 0x7FFFFFu);
+    const uint32_t body = e <= 0 ? 0u : (e >= 255 ? 0x7F800000u : ((uint32_t)e << 23) | mant);
+    return __uint_as_float(sign | body);
+}
+
 template <int D>
 struct dp_shadow_t;
 template <>

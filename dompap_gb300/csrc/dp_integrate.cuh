@@ -24,6 +24,7 @@ struct dp_int_args {
     const void* shadow_ref;
     const uint8_t* mclass;  // massmode 1: mass class per particle
     const double* mcoef;    // massmode 1: [class][5]: a, b dt/m, b/(2m), sqrt(2 alpha T dt), dt/m
+    const float2* mcoef_f;  // massmode 1: [class]: float32 b/(2m), sqrt(2 alpha T dt)
     const double* mass;     // massmode 2: mass per particle
     dp_dev_status* st;
     long long n;
@@ -34,6 +35,7 @@ struct dp_int_args {
     float thr_lo, thr_hi;        // float32 bracket of thr for the shadow test
     double dt;
     double coef[5];              // massmode 0
+    float coef_f[2];             // massmode 0: float32 coef[2], coef[3] (the noise terms)
     double temperature;
     double tau;
     unsigned long long seed;
@@ -58,17 +60,26 @@ __device__ __forceinline__ void dp_gjf_coefficients(double m, double dt, double 
     c[4] = dt / m;
 }
 
+// c: the five float64 coefficients; cf: float32 b/(2m) and sqrt(2 alpha T dt)
+// for the noise terms.
 template <int MASSMODE>
-__device__ __forceinline__ void dp_load_coef(const dp_int_args& a, long long i, double* c) {
+__device__ __forceinline__ void dp_load_coef(const dp_int_args& a, long long i, double* c, float* cf) {
     if (MASSMODE == 0) {
 #pragma unroll
         for (int t = 0; t < 5; ++t) c[t] = a.coef[t];
+        cf[0] = a.coef_f[0];
+        cf[1] = a.coef_f[1];
     } else if (MASSMODE == 1) {
         const int cl = a.mclass[i];
 #pragma unroll
         for (int t = 0; t < 5; ++t) c[t] = __ldg(a.mcoef + cl * 5 + t);
+        const float2 f = __ldg(a.mcoef_f + cl);
+        cf[0] = f.x;
+        cf[1] = f.y;
     } else {
         dp_gjf_coefficients(a.mass[i], a.dt, a.temperature, a.tau, c);
+        cf[0] = (float)c[2];
+        cf[1] = (float)c[3];
     }
 }
 
@@ -114,7 +125,12 @@ __device__ __forceinline__ bool dp_skin_old(const void* shadow_ref, const double
 // Langevin G-JF leap-frog (dompap/integrator.py:17-40, arXiv:1303.7011
 // Sec. II.C eqs. 16-17) or NVE leap-frog (:5-14) of particle i with force F,
 // then the wrap into the box, the fixed-point forms and the skin test (the
-// return value). The float64 position is converted to fixed point once: one
+// return value). The deterministic part a v + (b dt / m) F is float64 (two
+// fused multiply-adds); the noise terms beta_new = sqrt(2 alpha T dt) z and
+// b (beta_old + beta_new) / (2m) are float32, like the float32 normal deviate
+// z they scale (relative error ~1e-7 on a random term): this GPU runs float64
+// at 1/64 of the float32 rate, and the integrator's float64 work bounds the
+// step once the pair loop is cheap. The float64 position is converted to fixed point once: one
 // product p = x 2^64 / L gives the wrap test (its bit pattern), the 64-bit
 // fixed point and the 32-bit shadow (its upper word). `bad` is set when a
 // coordinate is not finite.
@@ -122,7 +138,8 @@ template <int D, int MASSMODE, bool NVE, bool WRITE64>
 __device__ __forceinline__ bool dp_integrate_one(const dp_int_args& a, long long i, const double* F, bool& bad) {
     const long long n = a.n;
     double c[5];
-    dp_load_coef<MASSMODE>(a, i, c);
+    float cf[2];
+    dp_load_coef<MASSMODE>(a, i, c, cf);
     float z[4];
     if (!NVE) dp_normals4(a.seed, (unsigned long long)(a.st->step + a.step_offset), (uint32_t)i, z);
     // every load is issued before the first store (the arrays are not
@@ -147,9 +164,11 @@ __device__ __forceinline__ bool dp_integrate_one(const dp_int_args& a, long long
         if (NVE) {
             v = v + c[4] * F[k];  // make_one_step_leap_frog (dompap/integrator.py:12)
         } else {
-            const double bn = c[3] * dp_f2d(z[k]);
-            v = c[0] * v + c[1] * F[k] + c[2] * (bin[k] + bn);
-            a.beta[o] = bn;
+            // separately rounded float32 operations (no contraction)
+            const float bn = __fmul_rn(cf[1], z[k]);
+            const float noise = __fmul_rn(cf[0], __fadd_rn(dp_d2f_trunc(bin[k]), bn));
+            v = fma(c[1], F[k], fma(c[0], v, dp_f2d(noise)));
+            a.beta[o] = dp_f2d(bn);
         }
         x = x + v * a.dt;
         double p = x * a.scale64[k];

@@ -232,6 +232,12 @@ int dp_batch_run(dp_batch *batch, int64_t steps, int sample_every, int nve, int 
  * (may be NULL) receives the CUBIN size. */
 int dp_nvrtc_check(int dim, int precision, int pair_mode, int with_batch, const char *device_source,
                    int64_t *cubin_bytes);
+/* The same compile with the assembler's verbose report: registers, spill
+ * stores/loads and shared memory of every kernel of the program, written to
+ * log (NUL-terminated, truncated to log_capacity); log_bytes (may be NULL)
+ * receives the full length. Host only (no counterpart in the reference). */
+int dp_nvrtc_resources(int dim, int precision, int pair_mode, int with_batch, const char *device_source, char *log,
+                       int64_t log_capacity, int64_t *log_bytes);
 /* Verlet lists for the batch (replaces the per-step 27-cell stencil; no
  * counterpart in the reference, whose replicas each run dompap's own list,
  * dompap/neighbor_list.py:7-201): partners within r_cut + skin, rebuilt per

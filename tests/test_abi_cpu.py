@@ -123,3 +123,32 @@ def test_nvrtc_programs_compile(dim, precision, pmode, batch):
     rc = _lib.load().dp_nvrtc_check(dim, precision, pmode, batch, src.encode(), ctypes.byref(size))
     assert rc == 0, _lib.load().dp_last_error().decode()
     assert size.value > 10000
+
+
+def test_nvrtc_resource_report():
+    """The assembler's verbose report of a run-time program: every kernel's
+    registers, spills and shared memory (the fused step is built for six
+    resident 256-thread CTAs per SM, so at most 40 registers)."""
+    import ctypes
+    import re
+
+    from dompap_gb300 import _lib, codegen
+
+    src, _ = codegen.make_pair_source("(1-r)**2", 1.0)
+    buf = ctypes.create_string_buffer(1 << 18)
+    size = ctypes.c_int64(0)
+    rc = _lib.load().dp_nvrtc_resources(3, 0, 0, 0, src.encode(), buf, len(buf), ctypes.byref(size))
+    assert rc == 0, _lib.load().dp_last_error().decode()
+    text = buf.value.decode()
+    assert 0 < size.value <= len(buf)
+    used = {}
+    kernel = None
+    for line in text.splitlines():
+        m = re.search(r"entry function '(\w+)'", line)
+        if m:
+            kernel = m.group(1)
+        m = re.search(r"Used (\d+) registers", line)
+        if m and kernel:
+            used[kernel] = int(m.group(1))
+    assert {"dp_forces", "dp_step", "dp_energy", "dp_virial"} <= set(used)
+    assert used["dp_step"] <= 40

@@ -58,9 +58,25 @@ def test_gjf_tau_inf_trajectory(golden_traj):
     assert np.array_equal(sim.image_positions, t["images"])
 
 
-def test_gjf_step_arithmetic():
+def _d2f_trunc(x):
+    """float64 -> float32 truncating the mantissa (the kernel's bit move)."""
+    b = np.ascontiguousarray(x, dtype=np.float64).view(np.uint64)
+    e = ((b >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64) - 1023 + 127
+    sign = ((b >> np.uint64(63)).astype(np.uint32)) << np.uint32(31)
+    mant = ((b >> np.uint64(29)) & np.uint64(0x7FFFFF)).astype(np.uint32)
+    body = np.where(e <= 0, np.uint32(0),
+                    np.where(e >= 255, np.uint32(0x7F800000),
+                             (np.clip(e, 0, 255).astype(np.uint32) << np.uint32(23)) | mant))
+    return (sign | body.astype(np.uint32)).view(np.float32)
+
+
+@pytest.mark.parametrize("masses", ["classes", "one"])
+def test_gjf_step_arithmetic(masses):
     """One G-JF step on the GPU equals make_one_step (dompap/integrator.py:17-40)
-    fed with the GPU's own normal deviates for that step."""
+    fed with the GPU's own normal deviates for that step: the deterministic
+    part a v + (b dt / m) F to float64 rounding, the noise terms
+    beta_new = sqrt(2 alpha T dt) z and b (beta_old + beta_new) / (2m) exactly
+    as their float32 products and sum."""
     from dompap_gb300 import Simulation
     from dompap_gb300 import _lib
 
@@ -69,7 +85,10 @@ def test_gjf_step_arithmetic():
     sim.set_positions(unit_cell_coordinates=([0, 0, 0], [0.5, 0.5, 0.5]), cells=(5, 5, 5),
                       lattice_constants=(1, 1, 1))
     n = sim.number_of_particles()
-    sim.set_masses(masses=list(rng.choice([1.0, 2.0, 0.5], size=n)))
+    if masses == "classes":
+        sim.set_masses(masses=list(rng.choice([1.0, 2.0, 0.5], size=n)))
+    else:
+        sim.set_masses(masses=1.5)
     sim.set_density(density=1.1)
     sim.positions = sim.positions + rng.normal(0, 0.05, size=sim.positions.shape)
     sim.wrap_into_box()
@@ -77,7 +96,8 @@ def test_gjf_step_arithmetic():
     sim.betas = rng.normal(scale=0.1, size=(n, 3))
     sim.set_pair_potential("(1-r)**2", 1.0)
     sim.set_neighbor_list(skin=0.3)
-    sim.set_integrator(time_step=0.01, target_temperature=0.7, temperature_damping_time=0.2)
+    dt, temp, tau = 0.01, 0.7, 0.2
+    sim.set_integrator(time_step=dt, target_temperature=temp, temperature_damping_time=tau)
     pos0, vel0, beta0 = np.array(sim.positions), np.array(sim.velocities), np.array(sim.betas)
     img0 = np.array(sim.image_positions)
     forces = sim.get_forces()
@@ -85,11 +105,24 @@ def test_gjf_step_arithmetic():
     normals = np.empty((n, 3))
     _lib.check(_lib.load().dp_get_normals(sim._h, step, _lib.dptr(normals)))
     sim.step()
-    pos, vel, beta = ref.gjf_step(pos0, vel0, beta0, forces, np.array(sim.masses), 0.01, 0.7, 0.2, normals)
+    m = np.array(sim.masses).reshape(n, 1)
+    # the reference's coefficients (dompap/integrator.py:29-36)
+    alpha = m / tau
+    denominator = 1.0 + alpha * dt / 2.0 / m
+    b = 1 / denominator
+    c2 = (b / 2 / m).astype(np.float32)
+    c3 = np.sqrt(2 * alpha * temp * dt).astype(np.float32)
+    bn = c3 * normals.astype(np.float32)
+    noise = c2 * (_d2f_trunc(beta0).reshape(n, 3) + bn)
+    assert bn.dtype == np.float32 and noise.dtype == np.float32
+    # deterministic part: make_one_step with both noise terms zero
+    _, vel_det, _ = ref.gjf_step(pos0, vel0, np.zeros_like(beta0), forces, m, dt, temp, tau, np.zeros_like(normals))
+    vel = vel_det + noise.astype(np.float64)
+    pos = pos0 + vel * dt
     img = img0.copy()
     ref.wrap_into_box(pos, img, np.array(sim.box_vectors))
+    assert np.array_equal(sim.betas, bn.astype(np.float64))
     assert np.max(np.abs(sim.velocities - vel)) <= 1e-13
-    assert np.max(np.abs(sim.betas - beta)) <= 1e-13
     assert np.max(np.abs(sim.positions - pos)) <= 1e-13
     assert np.array_equal(sim.image_positions, img)
 
