@@ -15,7 +15,8 @@
 //      of the launch (binning every step), so no pair is ever missed;
 //   2. pair forces in float32 from the fixed-point displacements of the
 //      listed partners, the replica's positions read from shared memory;
-//   3. G-JF (or NVE) leap-frog in float64 as dompap/integrator.py:17-40, wrap
+//   3. G-JF (or NVE) leap-frog as dompap/integrator.py:17-40 (deterministic
+//      part float64, noise terms float32 as in dp_integrate.cuh), wrap
 //      as dompap/positions.py:90-98, new fixed-point position to HBM.
 // Every `sample_every` steps the CTA adds U, W and sum m v^2 of the replica to
 // its observable slots (float64).
@@ -130,6 +131,8 @@ __device__ __forceinline__ void dp_batch_steps(const dp_batch_args& a) {
         double c[5];
 #pragma unroll
         for (int t = 0; t < 5; ++t) c[t] = a.coef[r * 5 + t];
+        // the noise terms in float32, as the single-system integrator
+        const float c2f = (float)c[2], c3f = (float)c[3];
         // list of this replica: column-major, n rows
         uint16_t* __restrict__ nl = a.nlist ? a.nlist + off * (long long)a.kmax : nullptr;
         bool use_list = nl != nullptr;  // cleared for the rest of the launch if the list overflows
@@ -282,9 +285,10 @@ __device__ __forceinline__ void dp_batch_steps(const dp_batch_args& a) {
                     if (a.nve) {
                         v = v + c[4] * F;
                     } else {
-                        const double bn = c[3] * (double)z[k];
-                        v = c[0] * v + c[1] * F + c[2] * (a.beta[o] + bn);
-                        a.beta[o] = bn;
+                        const float bn = __fmul_rn(c3f, z[k]);
+                        const float noise = __fmul_rn(c2f, __fadd_rn(dp_d2f_trunc(a.beta[o]), bn));
+                        v = fma(c[1], F, fma(c[0], v, dp_f2d(noise)));
+                        a.beta[o] = dp_f2d(bn);
                     }
                     x = x + v * a.dt;
                     const long long t = __double2ll_rd(x * scale[k]);
