@@ -244,7 +244,8 @@ def _block_mean(x, nblocks=10):
 def test_lj_ensemble_matches_oracle():
     """LJ fcc 500 at density 0.8442, T = 1 (the CPU-runnable case): ensemble
     means of T, U/N and P from the GPU run and from the oracle's own Langevin
-    run agree within 4 combined standard errors (block averages)."""
+    run agree within 4 combined standard errors (block averages), and so does
+    g(r) bin by bin (5 standard errors, the first peak in the same bin)."""
     from dompap_gb300 import Simulation
     from dompap_gb300.positions import FCC
 
@@ -261,18 +262,20 @@ def test_lj_ensemble_matches_oracle():
     pos0, vel0, box = np.array(sim.positions), np.array(sim.velocities), np.array(sim.box_vectors)
     n = pos0.shape[0]
     equil, samples, stride = 600, 160, 10
+    r_bins = np.linspace(0.0, 0.5 * float(box[0]), 61)
     sim.run(equil)
-    g = {"T": [], "U": [], "P": []}
+    g = {"T": [], "U": [], "P": [], "rdf": []}
     for _ in range(samples):
         sim.run(stride)
         g["T"].append(sim.get_temperature())
         g["U"].append(sim.get_potential_energy() / n)
         g["P"].append(sim.get_pressure())
+        g["rdf"].append(sim.get_radial_distribution_function(r_bins)[1])
     o = ref.OracleSystem(pos0, vel0, np.ones(n), box, "4*(r**-12-r**-6)", 2.5, 0.5, max_neighbors=256)
     o.dt, o.temperature, o.damping_time = 0.005, 1.0, 0.1
     for _ in range(equil):
         o.step_gjf(rng.normal(size=(n, 3)))
-    h = {"T": [], "U": [], "P": []}
+    h = {"T": [], "U": [], "P": [], "rdf": []}
     for _ in range(samples):
         for _ in range(stride):
             o.step_gjf(rng.normal(size=(n, 3)))
@@ -283,8 +286,22 @@ def test_lj_ensemble_matches_oracle():
         w = ref.virial_double_loop(o.positions, box, o.f)
         vol = float(np.prod(box))
         h["P"].append(w / vol + np.sum(o.velocities ** 2) / 3 / vol)
+        h["rdf"].append(ref.radial_distribution_function(o.positions, o.positions, box, r_bins)[1])
     for key in ("T", "U", "P"):
         mg, eg = _block_mean(g[key])
         mo, eo = _block_mean(h[key])
         print(f"{key}: GPU {mg:.4f} +- {eg:.4f}   oracle {mo:.4f} +- {eo:.4f}")
         assert abs(mg - mo) < 4 * np.hypot(eg, eo) + 1e-3 * abs(mo), key
+    # g(r): block means per bin
+    blocks_g = np.array([b.mean(axis=0) for b in np.array_split(np.array(g["rdf"]), 10)])
+    blocks_o = np.array([b.mean(axis=0) for b in np.array_split(np.array(h["rdf"]), 10)])
+    mg, mo = blocks_g.mean(axis=0), blocks_o.mean(axis=0)
+    err = np.hypot(blocks_g.std(axis=0, ddof=1), blocks_o.std(axis=0, ddof=1)) / np.sqrt(10)
+    z = np.abs(mg - mo) / (err + 1e-3)
+    # the first peak beyond the self pairs (dompap counts them, at r = 0)
+    shell = 0.5 * (r_bins[1:] + r_bins[:-1]) > 0.5
+    pg, po = np.argmax(np.where(shell, mg, 0.0)), np.argmax(np.where(shell, mo, 0.0))
+    print(f"g(r): first peak GPU {mg[pg]:.3f} at bin {pg}, oracle {mo[po]:.3f} at bin {po}; "
+          f"largest deviation {z.max():.2f} standard errors")
+    assert pg == po and mg[pg] > 2.0
+    assert z.max() < 5.0
