@@ -194,8 +194,9 @@ def kernel_times(sim, reps=50):
 
 
 def e2e_run(sim, steps):
-    """C-ABI step with host buffers: upload pos/vel/beta from pinned memory,
-    one step, download positions; device time from host clock with syncs."""
+    """C-ABI step with host buffers (dp_run_host): upload pos/vel/beta from
+    pinned memory, one step, download positions, every step; host clock
+    around the loop (each call ends with the device idle)."""
     import torch
 
     from dompap_gb300 import _lib
@@ -214,11 +215,8 @@ def e2e_run(sim, steps):
     _lib.check(lib.dp_get_betas(h, _lib.dptr(beta)))
     t0 = time.perf_counter()
     for _ in range(steps):
-        _lib.check(lib.dp_set_positions(h, _lib.dptr(pos)))
-        _lib.check(lib.dp_set_velocities(h, _lib.dptr(vel)))
-        _lib.check(lib.dp_set_betas(h, _lib.dptr(beta)))
-        _lib.check(lib.dp_run(h, 1, _lib.DP_INT_GJF))
-        _lib.check(lib.dp_get_positions(h, _lib.dptr(out)))
+        _lib.check(lib.dp_run_host(h, _lib.dptr(pos), _lib.dptr(vel), _lib.dptr(beta), 1, _lib.DP_INT_GJF,
+                                   _lib.dptr(out), None, None))
     dt = time.perf_counter() - t0
     sim._mark_device_newer()
     return n * steps / dt, 3 * n * d * 8, n * d * 8

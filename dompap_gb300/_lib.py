@@ -105,6 +105,7 @@ _SIGNATURES = {
     "dp_get_reference_positions": (ctypes.c_int, [_P, _D]),
     "dp_set_integrator": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_uint64]),
     "dp_run": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int]),
+    "dp_run_host": (ctypes.c_int, [_P, _D, _D, _D, ctypes.c_int64, ctypes.c_int, _D, _D, _D]),
     "dp_run_timed": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "dp_forces": (ctypes.c_int, [_P, _D]),
     "dp_potential_energy": (ctypes.c_int, [_P, _D]),

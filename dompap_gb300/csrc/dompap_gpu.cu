@@ -121,8 +121,11 @@ __device__ __forceinline__ unsigned long long fixed64_wrapped(double x, double L
     return dp_fixed64_of(x * scale64);
 }
 
-// Fixed-point shadow of all positions; flags coordinates outside
-// [-L/4, 5L/4), for which the single-shift image is not the nearest one.
+// Fixed-point forms of all positions (the 64-bit X of the position wrapped
+// into the box, the shadow its upper word, as the integrators write them);
+// flags coordinates outside [-L/4, 5L/4), for which the single-shift image is
+// not the nearest one. One float64 product per coordinate in the box: its
+// bit pattern is the in-box test.
 template <int D>
 __global__ void k_shadow(ShadowArgs a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -133,9 +136,15 @@ __global__ void k_shadow(ShadowArgs a) {
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         const double x = a.pos[k * a.n + i];
-        u[k] = dp_fixed(x, a.scale[k]);
-        X[k] = fixed64_wrapped(x, a.box[k], a.scale64[k]);
-        far = far || !(x >= -0.25 * a.box[k] && x < 1.25 * a.box[k]);
+        double p = x * a.scale64[k];
+        const long long pb = __double_as_longlong(p);
+        if (!(pb >= 0 && pb < 0x43F0000000000000LL)) {  // p outside [0, 2^64): wrap a copy
+            far = far || !(x >= -0.25 * a.box[k] && x < 1.25 * a.box[k]);
+            const double w = x - floor(x / a.box[k]) * a.box[k];
+            p = (w >= 0.0 && w < a.box[k]) ? w * a.scale64[k] : 0.0;
+        }
+        X[k] = dp_fixed64_of(p);
+        u[k] = (uint32_t)(X[k] >> 32);
     }
     ((typename dp_shadow_t<D>::type*)a.shadow)[i] = dp_shadow_pack<D>(u);
     ((typename dp_fixed64_t<D>::type*)a.pos64)[i] = dp_fixed64_pack<D>(X);
@@ -1821,7 +1830,8 @@ static int upload_aos_f64(dp_sim* s, const double* host, double* dev_soa) {
     return DP_OK;
 }
 
-static int download_aos_f64(dp_sim* s, const double* dev_soa, double* host) {
+// device SoA -> host AoS (n, dim); the caller synchronises before reading it.
+static int download_aos_f64_async(dp_sim* s, const double* dev_soa, double* host) {
     if (!host) return fail(DP_ERR_ARG, "null array");
     const unsigned g = grid_for(s->n * s->dim, kBlock);
     if (double* view = (double*)mapped_view(host)) {
@@ -1833,6 +1843,11 @@ static int download_aos_f64(dp_sim* s, const double* dev_soa, double* host) {
         CK(cudaMemcpyAsync(host, s->bk_vel, (size_t)s->n * s->dim * sizeof(double), cudaMemcpyDeviceToHost,
                            s->stream));
     }
+    return DP_OK;
+}
+
+static int download_aos_f64(dp_sim* s, const double* dev_soa, double* host) {
+    RET(download_aos_f64_async(s, dev_soa, host));
     CK(cudaStreamSynchronize(s->stream));
     return DP_OK;
 }
@@ -2165,6 +2180,25 @@ int dp_run(dp_sim* s, int64_t steps, int kind) { return run_impl(s, steps, kind,
 int dp_run_timed(dp_sim* s, int64_t steps, int kind, float* ms) {
     if (!ms) return fail(DP_ERR_ARG, "ms is null");
     return run_impl(s, steps, kind, ms);
+}
+
+int dp_run_host(dp_sim* s, const double* positions, const double* velocities, const double* betas, int64_t steps,
+                int kind, double* positions_out, double* velocities_out, double* betas_out) {
+    RET(require_ready(s));
+    // uploads, run and downloads are ordered on the stream; the host waits
+    // inside run() (its status reads) and once after the downloads
+    if (positions) {
+        RET(upload_aos_f64_async(s, positions, s->pos));
+        RET(launch_shadow(s));
+    }
+    if (velocities) RET(upload_aos_f64_async(s, velocities, s->vel));
+    if (betas) RET(upload_aos_f64_async(s, betas, s->beta));
+    RET(run_impl(s, steps, kind, nullptr));
+    if (positions_out) RET(download_aos_f64_async(s, s->pos, positions_out));
+    if (velocities_out) RET(download_aos_f64_async(s, s->vel, velocities_out));
+    if (betas_out) RET(download_aos_f64_async(s, s->beta, betas_out));
+    CK(cudaStreamSynchronize(s->stream));
+    return DP_OK;
 }
 
 // --------------------------- observables ----------------------------------

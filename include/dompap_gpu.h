@@ -130,6 +130,15 @@ int dp_set_integrator(dp_sim *sim, double time_step, double temperature, double 
  * with make_one_step / make_one_step_leap_frog (dompap/integrator.py:5-40)
  * and wrap_into_box (dompap/positions.py:90-98). */
 int dp_run(dp_sim *sim, int64_t steps, int kind);
+/* dp_run on host arrays, as dompap's step keeps its state: the (N, D)
+ * float64 row-major positions, velocities and betas given (each may be NULL:
+ * kept) are uploaded, `steps` steps run, and the arrays asked for (each may
+ * be NULL) are written back; one call, one final wait. Replaces
+ * Simulation.step / run (dompap/Simulation.py:681-737) with its NumPy state
+ * arrays in and out (dompap/integrator.py:17-40 returns new arrays). Page-locked
+ * host arrays are read and written by the device directly. */
+int dp_run_host(dp_sim *sim, const double *positions, const double *velocities, const double *betas, int64_t steps,
+                int kind, double *positions_out, double *velocities_out, double *betas_out);
 /* Same as dp_run, also returning the device time of the steps in ms
  * (CUDA events on the handle's stream). */
 int dp_run_timed(dp_sim *sim, int64_t steps, int kind, float *ms);

@@ -277,3 +277,39 @@ def test_non_cubic_box_forces_and_steps():
     assert np.max(np.abs(sim.positions - o.positions)) <= 1e-11
     assert np.array_equal(sim.image_positions, o.images)
     assert rel_rms(sim.get_forces(), o.forces()) <= TOL
+
+
+def test_run_host_equals_setters_run_getters(golden_configs):
+    """dp_run_host (host state in, steps, host state out in one call) gives
+    bit-identical results to the separate setters, run and getters."""
+    from dompap_gb300 import _lib
+
+    cfg = config_of(golden_configs, "lj500")
+    out = []
+    for combined in (False, True):
+        np.random.seed(77)
+        sim = sim_from_config(cfg, "lj500", method="cell list")
+        sim.set_integrator(time_step=0.004, target_temperature=1.2, temperature_damping_time=0.2)
+        sim.run(5)
+        lib, h = _lib.load(), sim._h
+        n = sim.number_of_particles()
+        rng = np.random.default_rng(3)
+        pos = np.ascontiguousarray(np.array(sim.positions) + rng.normal(0, 1e-3, size=(n, 3)))
+        vel = np.ascontiguousarray(rng.normal(0, 1.0, size=(n, 3)))
+        beta = np.ascontiguousarray(rng.normal(0, 0.1, size=(n, 3)))
+        p_out, v_out, b_out = np.empty((n, 3)), np.empty((n, 3)), np.empty((n, 3))
+        if combined:
+            _lib.check(lib.dp_run_host(h, _lib.dptr(pos), _lib.dptr(vel), _lib.dptr(beta), 7, _lib.DP_INT_GJF,
+                                       _lib.dptr(p_out), _lib.dptr(v_out), _lib.dptr(b_out)))
+        else:
+            _lib.check(lib.dp_set_positions(h, _lib.dptr(pos)))
+            _lib.check(lib.dp_set_velocities(h, _lib.dptr(vel)))
+            _lib.check(lib.dp_set_betas(h, _lib.dptr(beta)))
+            _lib.check(lib.dp_run(h, 7, _lib.DP_INT_GJF))
+            _lib.check(lib.dp_get_positions(h, _lib.dptr(p_out)))
+            _lib.check(lib.dp_get_velocities(h, _lib.dptr(v_out)))
+            _lib.check(lib.dp_get_betas(h, _lib.dptr(b_out)))
+        sim._mark_device_newer()
+        out.append((p_out, v_out, b_out))
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
