@@ -2,3 +2,5 @@
 
 from .autotune import autotune  # noqa: F401
 from .progress_bar import progress_bar  # noqa: F401
+from .run_test_simulation import run_test_simulation  # noqa: F401
+from .to_lammps_dump import to_lammps_dump  # noqa: F401

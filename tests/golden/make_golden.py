@@ -6,7 +6,7 @@ Run in a checkout that has the reference source next to it::
 
     python tests/golden/make_golden.py [--reference PATH]
 
-It writes ``golden_*.npz`` and ``checkpoint_ref.csv/.toml``. Every array is produced by calling the reference's
+It writes ``golden_*.npz``, ``checkpoint_ref.csv/.toml`` and ``lammps_ref.*``. Every array is produced by calling the reference's
 own functions / ``Simulation`` methods on seeded inputs; nothing here restates
 the reference's arithmetic. The fixtures are what ``tests/`` pin the oracle and
 the CUDA path against, on machines where the reference is absent.
@@ -130,10 +130,73 @@ def make_checkpoint(Simulation):
     print("checkpoint_ref.csv / .toml:", n, "particles")
 
 
+def make_lammps(Simulation):
+    """The reference's ``tools.to_lammps_dump`` text for a small seeded 3-D
+    binary system (types, masses, velocities, images, forces), the inputs it
+    read, and whether it raises for a 2-D system."""
+    from dompap.tools import to_lammps_dump
+
+    rng = np.random.default_rng(91)
+    sim = Simulation()
+    sim.set_positions(unit_cell_coordinates=FCC, cells=(2, 2, 2), lattice_constants=(1.0, 1.0, 1.0))
+    n = sim.number_of_particles()
+    sim.set_masses(masses=1.0)
+    sim.set_types([0, 1] * (n // 2))
+    sim.set_density(density=0.9)
+    sim.set_pair_potential(pair_potential_str=LJ, r_cut=1.5)
+    sim.set_neighbor_list(skin=0.3, max_number_of_neighbors=64)
+    sim.velocities = rng.normal(0.0, 0.7, size=sim.positions.shape)
+    sim.masses = rng.uniform(0.5, 2.0, size=(n, 1))
+    sim.image_positions = rng.integers(-3, 4, size=sim.positions.shape).astype(np.int32)
+    sim.positions = sim.positions + rng.normal(0.0, 0.02, size=sim.positions.shape)
+    sim.number_of_steps = 1234
+    forces = sim.get_forces()
+    diameters = sim.get_diameters()
+    # The tool converts one-element rows with int()/float(), which NumPy 2.5
+    # rejects for the (N, 1) arrays the Simulation holds; it is fed the same
+    # values as (N,) arrays (what int()/float() of a row returned on the NumPy
+    # it was written for).
+    from types import SimpleNamespace
+
+    proxy = SimpleNamespace(number_of_steps=sim.number_of_steps, box_vectors=sim.box_vectors,
+                            particle_types=sim.particle_types.reshape(-1), masses=sim.masses.reshape(-1),
+                            get_diameters=lambda: diameters.reshape(-1), positions=sim.positions,
+                            image_positions=sim.image_positions, velocities=sim.velocities,
+                            get_forces=lambda: forces)
+    text = to_lammps_dump(proxy)
+    with open(os.path.join(HERE, "lammps_ref.txt"), "w") as fh:
+        fh.write(text)
+    np.savez(os.path.join(HERE, "lammps_ref.npz"), positions=sim.positions, velocities=sim.velocities,
+             image_positions=sim.image_positions, particle_types=sim.particle_types, masses=sim.masses,
+             box_vectors=sim.box_vectors, diameters=diameters, forces=forces,
+             number_of_steps=np.int64(sim.number_of_steps))
+    sim2 = Simulation()
+    sim2.set_positions(unit_cell_coordinates=((0.0, 0.0),), cells=(3, 3), lattice_constants=(1.0, 1.0))
+    sim2.set_masses(masses=1.0)
+    sim2.set_density(density=0.9)
+    sim2.set_pair_potential(pair_potential_str=LJ, r_cut=1.5)
+    sim2.set_neighbor_list(skin=0.3, max_number_of_neighbors=64)
+    f2 = sim2.get_forces()
+    d2 = sim2.get_diameters()
+    proxy2 = SimpleNamespace(number_of_steps=0, box_vectors=sim2.box_vectors,
+                             particle_types=sim2.particle_types.reshape(-1), masses=sim2.masses.reshape(-1),
+                             get_diameters=lambda: d2.reshape(-1), positions=sim2.positions,
+                             image_positions=sim2.image_positions, velocities=sim2.velocities,
+                             get_forces=lambda: f2)
+    try:
+        to_lammps_dump(proxy2)
+        raised = ""
+    except ValueError as exc:
+        raised = str(exc)
+    with open(os.path.join(HERE, "lammps_ref_2d_error.txt"), "w") as fh:
+        fh.write(raised)
+    print("lammps_ref.txt:", n, "particles; 2-D raises:", repr(raised))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--only", choices=["checkpoint"], default=None,
+    ap.add_argument("--only", choices=["checkpoint", "lammps"], default=None,
                     help="regenerate only the named fixture")
     args = ap.parse_args()
     dompap = import_reference(args.reference)
@@ -141,6 +204,11 @@ def main():
         from dompap import Simulation
 
         make_checkpoint(Simulation)
+        return
+    if args.only == "lammps":
+        from dompap import Simulation
+
+        make_lammps(Simulation)
         return
     from dompap import Simulation
     from dompap import neighbor_list as rnl
