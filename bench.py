@@ -389,8 +389,20 @@ def batched_variant(seed, steps=40, warmup=5, loop_sample=16):
         loop_seconds += time.perf_counter() - t0
         loop_particles += n * steps
         del sim
+    # the plain single-system kernel on the same physics: one LJ system of
+    # 1,048,576 particles (fcc 64^3, density 0.8442, T = 1.35, the middle of the
+    # replicas' range), float64 parity and float32 forces
+    single = {}
+    for prec in ("fp64", "fp32"):
+        sim = _lattice_sim(FCC, (64, 64, 64), 0.8442, "4*(r**-12-r**-6)", 2.5, 0.5, 1.35, 0.005, 0.1, seed,
+                           0.02, precision=prec, kmax=256)
+        sim.run(warmup)
+        tms = sim.run_timed(20)
+        single[prec] = {"value": sim.number_of_particles() * 20 / (tms / 1000.0), "ms_per_step": tms / 20}
+        del sim
     return {"value": value, "unit": UNIT, "steps": steps, "ms_per_step": ms / steps, "replicas": reps.n_rep,
             "particles": reps.ntot, "rejected_draws_box_below_2rcut": rejected,
+            "single_system_lj_1M": dict(single, unit=UNIT, how="one 1,048,576-particle LJ system, fused step"),
             "launch_shape": {"split_n": best[0], "threads_small": best[1], "threads_large": best[2]},
             "force_rel_rms_error_vs_fp64_oracle_max": max(errs),
             "per_replica_loop": {"value": loop_particles / loop_seconds, "unit": UNIT,
