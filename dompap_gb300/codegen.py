@@ -61,14 +61,31 @@ def _hex(value: float) -> str:
     return f"R({float.hex(value)})"
 
 
+def _float32_exact(value: float) -> bool:
+    """A finite value that float32 holds exactly (normal range or zero)."""
+    if not np.isfinite(value):
+        return False
+    if value == 0.0:
+        return True
+    return 2.0 ** -126 <= abs(value) < 2.0 ** 127 and float(np.float32(value)) == value
+
+
 class _CudaPrinter(C99CodePrinter):
-    """C99 printer with ``R(...)`` literals and multiplication-chain powers."""
+    """C99 printer with ``R(...)`` literals and multiplication-chain powers;
+    constants float32 holds exactly are printed as ``dp_k<R>(...f)`` (the
+    double-float arithmetic multiplies and adds them as single floats)."""
 
     def _print_Float(self, expr):
-        return _hex(float(expr))
+        value = float(expr)
+        if _float32_exact(value):
+            return f"dp_k<R>({float.hex(value)}f)"
+        return _hex(value)
 
     def _print_Integer(self, expr):
-        return f"R({int(expr)})"
+        n = int(expr)
+        if abs(n) <= 2 ** 24:
+            return f"dp_k<R>({float(n)!r}f)"
+        return f"R({n})"
 
     def _print_Rational(self, expr):
         return f"(R({int(expr.p)})/R({int(expr.q)}))"
@@ -128,9 +145,24 @@ def _share_reciprocal(expr: sp.Expr) -> tuple[sp.Expr, bool]:
     return out, used
 
 
-def _function_source(name: str, expr: sp.Expr, shift_literal: str | None = None) -> str:
+def _horner(expr: sp.Expr) -> sp.Expr:
+    """A polynomial in one variable (r or 1/r) in Horner form: the force of
+    4 (r^-12 - r^-6), 48 r^-13 - 24 r^-7, becomes r^-7 (48 r^-6 - 24), with
+    fewer multiplications; anything else is returned as it is."""
+    syms = expr.free_symbols
+    if len(syms) != 1:
+        return expr
+    (x,) = syms
+    if not expr.is_polynomial(x):
+        return expr
+    return sp.horner(sp.expand(expr), wrt=x)
+
+
+def _function_source(name: str, expr: sp.Expr, shift_literal: str | None = None, horner: bool = False) -> str:
     printer = _CudaPrinter()
     expr, _ = _share_reciprocal(expr)
+    if horner:
+        expr = _horner(expr)
     repl, reduced = sp.cse(expr, symbols=sp.numbered_symbols("dp_t"))
     lines = [f"template <typename R> __device__ __forceinline__ R {name}(R r, R dp_inv_r) {{"]
     for sym, sub in repl:
@@ -174,7 +206,7 @@ def make_pair_source(pair_potential_str: str, r_cut: float) -> tuple[str, float]
         _PRELUDE,
         f"// u(r) = {pair_potential_str}   (r_cut = {r_cut!r}, u(r_cut) = {shift!r})",
         _function_source("dp_pair_u", u, shift_literal=_hex(shift)),
-        _function_source("dp_pair_f", f),
+        _function_source("dp_pair_f", f, horner=True),
         _function_source("dp_pair_c", c),
     ])
     return src, float(r_cut)

@@ -236,6 +236,20 @@ __device__ __forceinline__ float dp_d2f_trunc(double x) {
     return __uint_as_float(sign | body);
 }
 
+// A constant of a generated pair potential that float32 holds exactly
+// (dp_k<R>(48.0f)): R itself for float and double; the double-float
+// arithmetic (dp_ff.cuh) gives it a type whose products and sums take the
+// cheaper one-float forms.
+template <typename R>
+struct dp_k_t {
+    typedef R type;
+    static __device__ __forceinline__ R make(float v) { return R(v); }
+};
+template <typename R>
+__device__ __forceinline__ typename dp_k_t<R>::type dp_k(float v) {
+    return dp_k_t<R>::make(v);
+}
+
 template <int D>
 struct dp_shadow_t;
 template <>

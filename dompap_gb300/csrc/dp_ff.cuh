@@ -136,6 +136,25 @@ __device__ __forceinline__ void dpff_accumulate_prod(dpff& s, dpff x, dpff y) {
     s.lo += t.lo + pe;
 }
 
+// Exact float constants of generated expressions (dp_k<dpff>): x c and x + c
+// with one float operand.
+struct dpff_k {
+    float v;
+    __device__ __forceinline__ operator dpff() const { return dpff(v, 0.0f); }
+};
+template <>
+struct dp_k_t<dpff> {
+    typedef dpff_k type;
+    static __device__ __forceinline__ dpff_k make(float v) { return dpff_k{v}; }
+};
+__device__ __forceinline__ dpff operator*(dpff x, dpff_k k) { return dpff_mul_f(x, k.v); }
+__device__ __forceinline__ dpff operator*(dpff_k k, dpff x) { return dpff_mul_f(x, k.v); }
+__device__ __forceinline__ dpff operator+(dpff x, dpff_k k) { return dpff_add_f(x, k.v); }
+__device__ __forceinline__ dpff operator+(dpff_k k, dpff x) { return dpff_add_f(x, k.v); }
+__device__ __forceinline__ dpff operator-(dpff x, dpff_k k) { return dpff_add_f(x, -k.v); }
+__device__ __forceinline__ dpff operator-(dpff_k k, dpff x) { return dpff_add_f(-x, k.v); }
+__device__ __forceinline__ dpff_k operator-(dpff_k k) { return dpff_k{-k.v}; }
+
 // hi + lo in float64 with the two widenings done on bit patterns.
 __device__ __forceinline__ double dpff_to_double(dpff x) { return dp_f2d(x.hi) + dp_f2d(x.lo); }
 

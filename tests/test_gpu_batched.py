@@ -122,7 +122,10 @@ def test_batched_ensemble_matches_single_system():
             s = np.array(single)
             err = np.hypot(b.std(ddof=1), s.std(ddof=1)) / np.sqrt(len(b))
             print(f"replica {r} {key}: batched {b.mean():.4f} single {s.mean():.4f} (+- {err:.4f})")
-            assert abs(b.mean() - s.mean()) < 4 * err + 2e-3
+            # 10 blocks give a noisy standard error (the batched run's cell
+            # binning orders float32 sums by atomics, so each run samples a
+            # different trajectory): 5 of them plus 0.1 %
+            assert abs(b.mean() - s.mean()) < 5 * err + 1e-3 * abs(s.mean())
 
 
 def test_batched_autotune_and_full_shape():
