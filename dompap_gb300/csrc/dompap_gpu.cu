@@ -2009,21 +2009,23 @@ static std::string pair_program(int dim, int precision, int pmode, bool sig_one,
     return src;
 }
 
-// The fused step kernel is compiled for 6 resident 256-thread CTAs per SM (40
-// registers) with constant sigma/epsilon: there the spilled integrator tail
-// (~240 bytes) costs less than the occupancy buys (measured on GB300 against
-// 4, 5, 7 and 8). With per-type or per-pair tables the pair loop spills
-// ~600 bytes under that cap (the Wahnstrom mixture ran 17 % slower), so those
-// use 4 (64 registers).
-static int step_blocks_for(int dim, int pmode) {
-    (void)dim;
-    return pmode == DP_PAIR_CONST ? 6 : 4;
+// Resident 256-thread CTAs per SM the fused step kernel is compiled for
+// (measured on GB300 against 4, 5, 6, 7 and 8): 4 (64 registers) for the
+// double-float pair loop in 3 and 4 dimensions, whose pair terms spill under
+// a tighter cap (1M LJ particles: 0.99 ms per step against 1.10 with 6; 1M
+// harmonic: 3 % faster) and for per-type or per-pair tables (~600 bytes of
+// spills under 40 registers; the Wahnstrom mixture ran 17 % slower with 6);
+// 6 (40 registers) for the float32 pair loop and in 2 dimensions, where the
+// occupancy is worth more (7-8 % faster than with 4).
+static int step_blocks_for(int dim, int precision, int pmode) {
+    if (pmode != DP_PAIR_CONST) return 4;
+    return precision == DP_PREC_FP64 && dim >= 3 ? 4 : 6;
 }
 
 static int rebuild_pair_lib(dp_sim* s) {
     const bool sig_one = s->pmode == DP_PAIR_CONST && s->sigma == 1.0;
     const bool eps_one = s->pmode == DP_PAIR_CONST && s->epsilon == 1.0;
-    const int step_blocks = step_blocks_for(s->dim, s->pmode);
+    const int step_blocks = step_blocks_for(s->dim, s->precision, s->pmode);
     const std::string src =
         pair_program(s->dim, s->precision, s->pmode, sig_one, eps_one, s->pot_src, false, step_blocks);
     PairLib pl;
@@ -2992,7 +2994,7 @@ static int nvrtc_check_impl(int dim, int precision, int pair_mode, int with_batc
     if (pair_mode < DP_PAIR_CONST || pair_mode > DP_PAIR_DENSE) return fail(DP_ERR_ARG, "unknown pair mode");
     const bool one = pair_mode == DP_PAIR_CONST;
     const std::string src = pair_program(dim, precision, pair_mode, one, one, device_source, with_batch != 0,
-                                         step_blocks_for(dim, pair_mode));
+                                         step_blocks_for(dim, precision, pair_mode));
     std::vector<char> cubin;
     RET(nvrtc_cubin(src, &cubin, resource_log));
     if (cubin_bytes) *cubin_bytes = (int64_t)cubin.size();
