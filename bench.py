@@ -173,7 +173,7 @@ def measured_peaks():
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
 # measured by ncu on the melted state (step ~1400) of the named workload
-PROFILED_TRAFFIC_BYTES = {("harmonic3d", "step"): 316.5e6}
+PROFILED_TRAFFIC_BYTES = {("harmonic3d", "step"): 282.6e6}
 
 
 def kernel_times(sim, reps=50):
@@ -678,7 +678,7 @@ def main():
     if dominant in ("forces", "step"):
         line["roofline"]["note"] = ("float64-parity pair arithmetic runs in double-float on the FP32 pipes and "
                                     "the neighbour gathers are dependent loads: the kernel is latency bound "
-                                    "(long-scoreboard stalls; DRAM 38 %, no pipe above 35 % under ncu)")
+                                    "(long-scoreboard stalls; DRAM 35 %, no pipe above 35 % under ncu)")
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.workload, args.seed, steps_per_rebuild)
     if rank == 0 and not args.no_variants:
