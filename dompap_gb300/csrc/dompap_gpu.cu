@@ -805,7 +805,7 @@ struct dp_sim {
     int precision = DP_PREC_FP64;
     cudaStream_t stream = nullptr;
     cudaStream_t cstream = nullptr;  // captures the bodies of conditional graph nodes
-    bool conditional_graphs = true;  // cleared if the driver rejects conditional nodes
+    bool conditional_graphs = true;  // cleared if the CUDA driver rejects conditional nodes
     bool fused_step = true;          // run() uses dp_step (DOMPAP_FUSED_STEP=0: separate kernels)
     // surrogate pass: 0 = tcgen05 from 65,536 particles (the 128-particle CTAs
     // fill the GPU; on par with mma.sync there), mma.sync below; 1 = tcgen05;
@@ -1530,7 +1530,7 @@ static int record_steps(dp_sim* s, long long steps, int kind, cudaGraph_t graph,
     return DP_OK;
 }
 
-// Capture a chunk graph (conditional rebuild nodes when the driver takes
+// Capture a chunk graph (conditional rebuild nodes when the CUDA driver takes
 // them) and instantiate it.
 static int build_graph(dp_sim* s, long long steps, int kind, bool conditional, GraphEntry* g) {
     cudaGraph_t graph = nullptr;

@@ -9,7 +9,7 @@ network's error is kept uniform in f r); the GPU pair
 kernels then evaluate the cheap terms in float32 and the network on tensor
 cores (bf16 weights, fp32 accumulation). The network is trained on the GPU by
 the library's own forward/backward kernels (Adam) on samples of the
-code-generated float64 kernel, which stays the fallback and the judge
+code-generated float64 kernel, which stays the fallback and the yardstick
 (``PairSurrogate.errors``, force and NVE-drift comparisons in the tests and
 the benchmark).
 """

@@ -268,7 +268,7 @@ int dp_batch_last_forces(dp_batch *batch, double *forces);
  * accumulation on tensor cores (mma.sync m16n8k16), trained by the library's
  * own forward/backward kernels with Adam. No counterpart in dompap (it
  * evaluates every term through its jitted SymPy lambdas,
- * dompap/potential.py:43-66); the codegen path is its fallback and judge.
+ * dompap/potential.py:43-66); the codegen path is its fallback and yardstick.
  * Parameters (fp32, dp_mlp_param_count() of them): w1[64], b1[64],
  * W2[64][64] (row = output unit), b2[64], W3[2][64], b3[2]; norm[4]:
  * x_mean, 1/x_scale (x = (s - x_mean)/x_scale), u_scale, f_scale (of f r).
