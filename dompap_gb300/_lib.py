@@ -23,6 +23,7 @@ DP_ERR_OVERFLOW = 4
 DP_ERR_GEOMETRY = 5
 DP_ERR_NONFINITE = 6
 DP_ERR_NOPOT = 7
+DP_ERR_TIMEOUT = 8
 
 DP_PREC_FP64 = 0
 DP_PREC_FP32 = 1
@@ -49,6 +50,7 @@ _ERROR_NAMES = {
     DP_ERR_GEOMETRY: "invalid geometry",
     DP_ERR_NONFINITE: "non-finite force or position",
     DP_ERR_NOPOT: "no pair potential",
+    DP_ERR_TIMEOUT: "device-side wait timed out",
 }
 
 
@@ -105,6 +107,7 @@ _SIGNATURES = {
     "dp_get_reference_positions": (ctypes.c_int, [_P, _D]),
     "dp_set_integrator": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_uint64]),
     "dp_run": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int]),
+    "dp_selftest_bounded_wait": (ctypes.c_int, [_P, ctypes.c_int32]),
     "dp_run_host": (ctypes.c_int, [_P, _D, _D, _D, ctypes.c_int64, ctypes.c_int, _D, _D, _D]),
     "dp_run_timed": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "dp_forces": (ctypes.c_int, [_P, _D]),

@@ -34,6 +34,7 @@
 #include "dompap_gpu.h"
 #include "dp_common.cuh"
 #include "dp_integrate.cuh"
+#include "dp_umma.cuh"
 #include "dp_embedded.h"
 #include "mlp_common.cuh"
 #include "mlp_train.cuh"  // dp_src_common[], dp_src_pair[] (generated at build time)
@@ -407,6 +408,26 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_allpairs(NlArgs a) {
     for (int k = 0; k < D; ++k) a.pos_ref[k * n + i] = xi[k];
     typedef typename dp_shadow_t<D>::type sh_t;
     ((sh_t*)a.shadow_ref)[i] = ((const sh_t*)a.shadow)[i];
+}
+
+// Self-test of the bounded device-side waits, without a GPU fault: one CTA
+// allocates tensor memory as the surrogate pass does, waits on an mbarrier
+// that nothing arrives at, gives up after `limit` tries, frees the tensor
+// memory and records device_error (the host then reports DP_ERR_TIMEOUT).
+__global__ void __launch_bounds__(128) k_selftest_bounded_wait(dp_dev_status* st, int limit) {
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t s_tmem;
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) dp_mbar_init(&mbar, 1);
+    if (warp == 0) dp_tmem_alloc(&s_tmem, 64);
+    dp_tc_fence_before();
+    __syncthreads();
+    dp_tc_fence_after();
+    const bool arrived = dp_mbar_wait(&mbar, 0u, limit);
+    if (!arrived && threadIdx.x == 0) atomicExch(&st->device_error, 1);
+    dp_tc_fence_before();
+    __syncthreads();
+    if (warp == 0) dp_tmem_dealloc(s_tmem, 64);
 }
 
 __global__ void k_rebuild_done(dp_dev_status* st) {
@@ -1353,7 +1374,8 @@ static int check_device_error(dp_sim* s) {
     if (!s->hstat->device_error) return DP_OK;
     s->hstat->device_error = 0;
     RET(write_status(s));
-    return fail(DP_ERR_CUDA, "a device-side wait timed out in the tensor-core surrogate pass");
+    return fail(DP_ERR_TIMEOUT, "a bounded device-side wait gave up (tensor-core surrogate pass); the launch's "
+                                "results are discarded");
 }
 
 static int write_status(dp_sim* s) {
@@ -2178,6 +2200,15 @@ int dp_set_integrator(dp_sim* s, double time_step, double temperature, double da
 }
 
 int dp_run(dp_sim* s, int64_t steps, int kind) { return run_impl(s, steps, kind, nullptr); }
+
+int dp_selftest_bounded_wait(dp_sim* s, int32_t limit) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    if (limit < 1 || limit > (1 << 20)) return fail(DP_ERR_ARG, "limit must be in [1, 2^20]");
+    k_selftest_bounded_wait<<<1, 128, 0, s->stream>>>(s->dstat, limit);
+    CK(cudaGetLastError());
+    RET(read_status(s));
+    return check_device_error(s);
+}
 
 int dp_run_timed(dp_sim* s, int64_t steps, int kind, float* ms) {
     if (!ms) return fail(DP_ERR_ARG, "ms is null");

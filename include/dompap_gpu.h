@@ -31,6 +31,8 @@ extern "C" {
 #define DP_ERR_GEOMETRY 5   /* box too small for the single-image convention     */
 #define DP_ERR_NONFINITE 6  /* a force or position became NaN / Inf              */
 #define DP_ERR_NOPOT 7      /* no pair potential set                             */
+#define DP_ERR_TIMEOUT 8    /* a bounded device-side wait gave up; that launch's
+                               results are discarded, the context stays usable  */
 
 #define DP_PREC_FP64 0 /* float64 pair arithmetic (parity mode)                        */
 #define DP_PREC_FP32 1 /* float32 pair forces, float64 integration, wrap and sums      */
@@ -130,6 +132,12 @@ int dp_set_integrator(dp_sim *sim, double time_step, double temperature, double 
  * with make_one_step / make_one_step_leap_frog (dompap/integrator.py:5-40)
  * and wrap_into_box (dompap/positions.py:90-98). */
 int dp_run(dp_sim *sim, int64_t steps, int kind);
+/* Self-test of the bounded device-side waits (no counterpart in the
+ * reference): a kernel waits on an mbarrier that nothing arrives at, gives up
+ * after `limit` tries (1 .. 2^20), frees the tensor memory it holds and flags
+ * the failure; returns DP_ERR_TIMEOUT as a real timeout would, and the handle
+ * stays usable. No GPU fault is involved. */
+int dp_selftest_bounded_wait(dp_sim *sim, int32_t limit);
 /* dp_run on host arrays, as dompap's step keeps its state: the (N, D)
  * float64 row-major positions, velocities and betas given (each may be NULL:
  * kept) are uploaded, `steps` steps run, and the arrays asked for (each may
