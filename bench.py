@@ -545,7 +545,39 @@ def mlp_variant(seed, dim=3, steps=20, warmup=3, train_steps=100000):
     res["value"] = res["surrogate"]["value"]
     res["unit"] = UNIT
     del sim
+    res["nve_energy_drift"] = nve_drift_pair(sur, pot, dim, seed)
     return res
+
+
+def nve_drift_pair(sur, pot, dim, seed, steps=1000, blocks=5):
+    """Total-energy change per particle over `steps` NVE leap-frog steps
+    (dt = 0.002) of a small liquid of the same potential (melted with G-JF at
+    T = 1.5), with the float64 generated code and then with the surrogate from
+    the same state."""
+    from dompap_gb300.positions import FCC
+
+    unit, cells = (FCC, (10, 10, 10)) if dim == 3 else (BASIS_4D, (5, 5, 5, 5))
+    sim = _lattice_sim(unit, cells, 0.8, pot, 3.0, 0.3, 1.5, 0.004, 0.1, seed, 0.05,
+                       kmax=256 if dim == 3 else 512)
+    sim.run(400)
+    sim.set_integrator(time_step=0.002)
+    pos, vel, img = np.array(sim.positions), np.array(sim.velocities), np.array(sim.image_positions)
+
+    def drift():
+        e = [sim.get_potential_energy() + sim.get_kinetic_energy()]
+        for _ in range(blocks):
+            sim.run_leap_frog(steps // blocks)
+            e.append(sim.get_potential_energy() + sim.get_kinetic_energy())
+        n = sim.number_of_particles()
+        return {"change_per_particle": float((e[-1] - e[0]) / n), "std_per_particle": float(np.std(e) / n)}
+
+    out = {"particles": sim.number_of_particles(), "steps": steps, "time_step": 0.002,
+           "fp64_codegen": drift()}
+    sim.positions, sim.velocities, sim.image_positions = pos, vel, img
+    sim.set_pair_surrogate(sur)
+    out["surrogate"] = drift()
+    del sim
+    return out
 
 
 def variant_table(args):
