@@ -187,3 +187,31 @@ def test_surrogate_nve_drift_and_speed(surrogate):
           f"{msnn.value:.3f} ms")
     assert abs(dnn[0]) < 5e-3
     assert msnn.value < ms64.value
+
+
+def test_surrogate_ensemble_matches_float64_code(surrogate):
+    """Langevin ensemble averages (T, U/N, P) of the 4,000-particle liquid with
+    the surrogate agree with those of the float64 generated code within 4
+    combined standard errors (block averages of independent runs)."""
+
+    def ensemble(use_surrogate):
+        sim = _liquid(seed=6)
+        if use_surrogate:
+            sim.set_pair_surrogate(surrogate)
+        n = sim.number_of_particles()
+        sim.run(400)
+        obs = {"T": [], "U": [], "P": []}
+        for _ in range(100):
+            sim.run(20)
+            obs["T"].append(sim.get_temperature())
+            obs["U"].append(sim.get_potential_energy() / n)
+            obs["P"].append(sim.get_pressure())
+        return obs
+
+    a, b = ensemble(False), ensemble(True)
+    for key in ("T", "U", "P"):
+        ma = np.array([x.mean() for x in np.array_split(np.array(a[key]), 10)])
+        mb = np.array([x.mean() for x in np.array_split(np.array(b[key]), 10)])
+        err = np.hypot(ma.std(ddof=1), mb.std(ddof=1)) / np.sqrt(10)
+        print(f"{key}: float64 code {ma.mean():.4f}  surrogate {mb.mean():.4f}  (+- {err:.4f})")
+        assert abs(ma.mean() - mb.mean()) < 4 * err + 1e-3 * abs(ma.mean()), key
