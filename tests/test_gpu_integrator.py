@@ -305,3 +305,38 @@ def test_lj_ensemble_matches_oracle():
           f"largest deviation {z.max():.2f} standard errors")
     assert pg == po and mg[pg] > 2.0
     assert z.max() < 5.0
+
+
+def test_fp32_force_ensemble_matches_fp64():
+    """The FP32-force mode (float32 pair forces, float64 integration and sums)
+    samples the same Langevin ensemble as the float64-parity mode: T, U/N and
+    P of a 4,000-particle LJ liquid within 4 combined standard errors."""
+    from dompap_gb300 import Simulation
+    from dompap_gb300.positions import FCC
+
+    def ensemble(precision):
+        np.random.seed(8)
+        sim = Simulation(precision=precision)
+        sim.set_positions(unit_cell_coordinates=FCC, cells=(10, 10, 10), lattice_constants=(1, 1, 1))
+        sim.set_masses(masses=1.0)
+        sim.set_density(density=0.8442)
+        sim.set_random_velocities(temperature=1.2)
+        sim.set_pair_potential("4*(r**-12-r**-6)", 2.5)
+        sim.set_neighbor_list(skin=0.5, max_number_of_neighbors=256, method_str="cell list")
+        sim.set_integrator(time_step=0.005, target_temperature=1.2, temperature_damping_time=0.1)
+        n = sim.number_of_particles()
+        sim.run(1000)
+        obs = {"T": [], "U": [], "P": []}
+        for _ in range(100):
+            sim.run(20)
+            obs["T"].append(sim.get_temperature())
+            obs["U"].append(sim.get_potential_energy() / n)
+            obs["P"].append(sim.get_pressure())
+        return obs
+
+    a, b = ensemble("fp64"), ensemble("fp32")
+    for key in ("T", "U", "P"):
+        ma, ea = _block_mean(a[key])
+        mb, eb = _block_mean(b[key])
+        print(f"{key}: fp64 {ma:.4f} +- {ea:.4f}   fp32 {mb:.4f} +- {eb:.4f}")
+        assert abs(ma - mb) < 4 * np.hypot(ea, eb) + 1e-3 * abs(ma), key
