@@ -368,32 +368,50 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_cells(NlArgs a) {
 }
 
 // All-pairs build for boxes with fewer than 3 cells per axis; rows come out in
-// ascending index order, exactly the reference's double loop.
+// ascending index order, exactly the reference's double loop. As in the cell
+// build, the float32 shadow test decides every pair outside its error bracket
+// and float64 (the reference's test) only the rest.
 template <int D>
 __global__ void __launch_bounds__(kBlock) k_nl_build_allpairs(NlArgs a) {
     if (!a.st->need_rebuild) return;
+    typedef typename dp_shadow_t<D>::type sh_t;
     __shared__ double tile[D][kBlock];
+    __shared__ sh_t tsh[kBlock];
     const long long n = a.n;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < n;
+    const bool far = a.st->far != 0;
+    const sh_t* sh = (const sh_t*)a.shadow;
     double xi[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) xi[k] = active ? a.pos[k * n + i] : 0.0;
+    uint32_t ui[D];
+    dp_shadow_unpack<D>(active ? sh[i] : sh_t{}, ui);
     int count = 0;
     for (long long base = 0; base < n; base += kBlock) {
         const long long jl = base + threadIdx.x;
 #pragma unroll
         for (int k = 0; k < D; ++k) tile[k][threadIdx.x] = (jl < n) ? a.pos[k * n + jl] : 0.0;
+        tsh[threadIdx.x] = (jl < n) ? sh[jl] : sh_t{};
         __syncthreads();
         if (active) {
             const int lim = (int)min((long long)kBlock, n - base);
             for (int t = 0; t < lim; ++t) {
                 const long long j = base + t;
                 if (a.half ? j <= i : j == i) continue;
-                double d[D];
+                uint32_t uj[D];
+                dp_shadow_unpack<D>(tsh[t], uj);
+                float df[D];
+                const float qf = dp_shadow_q<D>(ui, uj, a.unit, df);
+                if (qf > a.hi2) continue;
+                bool inside = qf < a.lo2 && !far;
+                if (!inside) {
+                    double d[D];
 #pragma unroll
-                for (int k = 0; k < D; ++k) d[k] = dp_min_image(xi[k] - tile[k][t], a.box[k]);
-                if (sqrt(dp_sqsum_exact<D>(d)) < a.cutoff) {
+                    for (int k = 0; k < D; ++k) d[k] = dp_min_image(xi[k] - tile[k][t], a.box[k]);
+                    inside = sqrt(dp_sqsum_exact<D>(d)) < a.cutoff;
+                }
+                if (inside) {
                     if (count < a.kcap) a.nl[(long long)count * n + i] = (int32_t)j;
                     ++count;
                 }
@@ -406,8 +424,7 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_allpairs(NlArgs a) {
     atomicMax(&a.st->max_neighbors, count);
 #pragma unroll
     for (int k = 0; k < D; ++k) a.pos_ref[k * n + i] = xi[k];
-    typedef typename dp_shadow_t<D>::type sh_t;
-    ((sh_t*)a.shadow_ref)[i] = ((const sh_t*)a.shadow)[i];
+    ((sh_t*)a.shadow_ref)[i] = sh[i];
 }
 
 // Self-test of the bounded device-side waits, without a GPU fault: one CTA
