@@ -745,6 +745,8 @@ struct PairLib {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t forces = nullptr, energy = nullptr, virial = nullptr, laplacian = nullptr, eval = nullptr;
     cudaKernel_t step = nullptr;  // fused forces + integrate (not in the surrogate program)
+    cudaKernel_t step_warp = nullptr;  // the same, one warp per particle (small systems)
+    cudaKernel_t step_quad = nullptr;  // the same, four lanes per particle
     cudaKernel_t batch[4] = {nullptr, nullptr, nullptr, nullptr};  // 128, 256, 512, 1024 threads
     cudaKernel_t forces_mlp = nullptr, energy_mlp = nullptr, virial_mlp = nullptr, mlp_finish = nullptr;
     cudaKernel_t forces_mlp_tc = nullptr, energy_mlp_tc = nullptr, virial_mlp_tc = nullptr;  // tcgen05
@@ -802,7 +804,11 @@ static int compile_pair_lib(const std::string& src, PairLib* out) {
     CK(cudaLibraryGetKernel(&pl.virial, pl.lib, "dp_virial"));
     CK(cudaLibraryGetKernel(&pl.laplacian, pl.lib, "dp_laplacian"));
     CK(cudaLibraryGetKernel(&pl.eval, pl.lib, "dp_eval_pair"));
-    if (src.find("#define DP_MLP 1") == std::string::npos) CK(cudaLibraryGetKernel(&pl.step, pl.lib, "dp_step"));
+    if (src.find("#define DP_MLP 1") == std::string::npos) {
+        CK(cudaLibraryGetKernel(&pl.step, pl.lib, "dp_step"));
+        CK(cudaLibraryGetKernel(&pl.step_warp, pl.lib, "dp_step_warp"));
+        CK(cudaLibraryGetKernel(&pl.step_quad, pl.lib, "dp_step_quad"));
+    }
     if (src.find("#define DP_MLP 1") != std::string::npos) {
         CK(cudaLibraryGetKernel(&pl.forces_mlp, pl.lib, "dp_forces_mlp"));
         CK(cudaLibraryGetKernel(&pl.mlp_finish, pl.lib, "dp_mlp_forces_finish"));
@@ -845,6 +851,11 @@ struct dp_sim {
     cudaStream_t cstream = nullptr;  // captures the bodies of conditional graph nodes
     bool conditional_graphs = true;  // cleared if the CUDA driver rejects conditional nodes
     bool fused_step = true;          // run() uses dp_step (DOMPAP_FUSED_STEP=0: separate kernels)
+    // up to warp_step_max particles the fused step runs one warp per particle
+    // (dp_step_warp), up to quad_step_max four lanes per particle
+    // (dp_step_quad); DOMPAP_WARP_STEP / DOMPAP_QUAD_STEP set them (0: never)
+    long long warp_step_max = 8192;
+    long long quad_step_max = 65536;
     // surrogate pass: 0 = tcgen05 from 65,536 particles (the 128-particle CTAs
     // fill the GPU; on par with mma.sync there), mma.sync below; 1 = tcgen05;
     // 2 = mma.sync (DOMPAP_MLP_TENSOR=tcgen05 | mma)
@@ -1529,7 +1540,17 @@ static int launch_step(dp_sim* s, int kind, long long step_offset, long long* la
     ia.shadow_out = s->shadow_alt;
     ia.pos64_out = s->pos64_alt;
     void* args[] = {&pa, &ia};
-    CK(cudaLaunchKernel((const void*)s->lib.step, dim3(grid_for(s->n, kBlock)), dim3(kBlock), args, 0, s->stream));
+    if (s->n <= s->warp_step_max && s->lib.step_warp) {
+        // small system: one warp per particle (32 n threads)
+        CK(cudaLaunchKernel((const void*)s->lib.step_warp, dim3(grid_for(s->n * 32, kBlock)), dim3(kBlock), args, 0,
+                            s->stream));
+    } else if (s->n <= s->quad_step_max && s->lib.step_quad) {
+        CK(cudaLaunchKernel((const void*)s->lib.step_quad, dim3(grid_for(s->n * 4, kBlock)), dim3(kBlock), args, 0,
+                            s->stream));
+    } else {
+        CK(cudaLaunchKernel((const void*)s->lib.step, dim3(grid_for(s->n, kBlock)), dim3(kBlock), args, 0,
+                            s->stream));
+    }
     if (launches) *launches += 1;
     return DP_OK;
 }
@@ -1743,6 +1764,8 @@ int dp_create(int dim, int64_t n, int precision, dp_sim** out) {
     // that do not follow conditional graph nodes see every launch then)
     if (const char* env = std::getenv("DOMPAP_CONDITIONAL_GRAPHS")) s->conditional_graphs = std::atoi(env) != 0;
     if (const char* env = std::getenv("DOMPAP_FUSED_STEP")) s->fused_step = std::atoi(env) != 0;
+    if (const char* env = std::getenv("DOMPAP_WARP_STEP")) s->warp_step_max = std::atoll(env);
+    if (const char* env = std::getenv("DOMPAP_QUAD_STEP")) s->quad_step_max = std::atoll(env);
     if (const char* env = std::getenv("DOMPAP_MLP_TENSOR"))
         s->mlp_tensor = std::strcmp(env, "tcgen05") == 0 ? 1 : (std::strcmp(env, "mma") == 0 ? 2 : 0);
     int rc = DP_OK;

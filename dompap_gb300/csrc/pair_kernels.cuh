@@ -75,8 +75,12 @@ enum { DP_ACC_FORCE = 0, DP_ACC_ENERGY = 1, DP_ACC_VIRIAL = 2, DP_ACC_LAPLACE = 
 // some position is far outside the box, take the float64 path of the
 // reference instead (its min-image displacement, cut decision and pair
 // terms).
-template <int ACC>
-__device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long long i, double* f) {
+//
+// LANES > 1 (the fused step for small systems): LANES consecutive lanes share
+// particle i, lane `lane` of them taking list entries lane, lane + LANES, ...;
+// each returns its partial sums (the caller adds them across the group).
+template <int ACC, int LANES = 1>
+__device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long long i, double* f, int lane = 0) {
     constexpr int D = DP_DIM;
     const long long n = a.n;
     const shadow_t* __restrict__ sh = (const shadow_t*)a.shadow;
@@ -131,14 +135,16 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
     // as often as its busiest lane has kept neighbours, not once per listed
     // one (in a dense liquid with a thin skin most listed neighbours of most
     // lanes are outside r_cut at any step).
-    const int c = a.cnt[i];
-    const int32_t* __restrict__ row = a.nl + i;
+    const int c_all = a.cnt[i];
+    const int c = LANES > 1 ? (c_all > lane ? (c_all - lane + LANES - 1) / LANES : 0) : c_all;
+    const int32_t* __restrict__ row = a.nl + i + (LANES > 1 ? (long long)lane * n : 0LL);
+    const long long entry_stride = (long long)LANES * n;
     for (int base = 0; base < c; base += 32) {
         const int w = min(32, c - base);
         uint32_t kept = 0;
 #pragma unroll 4
         for (int t = 0; t < w; ++t) {
-            const int j = __ldg(row + (long long)(base + t) * n);
+            const int j = __ldg(row + (long long)(base + t) * entry_stride);
             // the virial is the reference's upper-triangle sum over n < m with
             // sigma(n, m), epsilon(n, m) (dompap/potential.py:265-278)
             if (ACC == DP_ACC_VIRIAL && j <= i) continue;
@@ -150,7 +156,7 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
         while (kept) {
             const int t = __ffs(kept) - 1;
             kept &= kept - 1;
-            const int j = __ldg(row + (long long)(base + t) * n);
+            const int j = __ldg(row + (long long)(base + t) * entry_stride);
             uint32_t uj[D];
 #if DP_FF
             unsigned long long Xj[D];
@@ -370,6 +376,46 @@ extern "C" __global__ void DP_STEP_BOUNDS dp_step(dp_pair_args a, dp_int_args b)
         if (any_bad) atomicExch(&b.st->nonfinite, 1);
     }
 }
+
+// The fused step for small systems: LANES lanes per particle. The lanes
+// split the particle's list (dp_particle_sum<..., LANES>), their partial
+// forces are added across the group in a fixed order, and the group's first
+// lane integrates. Below a few tens of thousands of particles this spreads the
+// pair loops over LANES times more threads than dp_step, whose one thread per
+// particle leaves most SMs idle.
+template <int LANES>
+__device__ __forceinline__ void dp_step_split(const dp_pair_args& a, const dp_int_args& b) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long i = t / LANES;
+    const int lane = (int)(t % LANES);
+    bool old = false, bad = false;
+    const bool active = i < a.n;  // uniform across the group, not the warp
+    double f[DP_DIM];
+#pragma unroll
+    for (int k = 0; k < DP_DIM; ++k) f[k] = 0.0;
+    if (active) dp_particle_sum<DP_ACC_FORCE, LANES>(a, i, f, lane);
+    // every lane of the warp takes part in the shuffles (groups past the
+    // last particle add zeros)
+#pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) {
+#pragma unroll
+        for (int k = 0; k < DP_DIM; ++k) f[k] += __shfl_down_sync(0xffffffffu, f[k], off, LANES);
+    }
+    if (active && lane == 0) {
+#pragma unroll
+        for (int k = 0; k < DP_DIM; ++k) bad = bad || !dp_isfinite_bits(f[k]);
+        old = dp_integrate_dispatch<DP_DIM, DP_FF != 0>(b, i, f, bad);
+    }
+    const bool any_old = __any_sync(0xffffffffu, old);
+    const bool any_bad = __any_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0) {
+        if (any_old) atomicExch(&b.st->need_rebuild, 1);
+        if (any_bad) atomicExch(&b.st->nonfinite, 1);
+    }
+}
+
+extern "C" __global__ void DP_STEP_BOUNDS dp_step_warp(dp_pair_args a, dp_int_args b) { dp_step_split<32>(a, b); }
+extern "C" __global__ void DP_STEP_BOUNDS dp_step_quad(dp_pair_args a, dp_int_args b) { dp_step_split<4>(a, b); }
 #endif
 
 // Per-block partial sums of a scalar pair quantity (energy or virial); the

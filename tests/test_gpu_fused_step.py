@@ -38,11 +38,15 @@ def test_fused_step_matches_separate_kernels(monkeypatch, golden_configs, tag, p
     a = _trajectory(monkeypatch, golden_configs, tag, True, precision, nve)
     b = _trajectory(monkeypatch, golden_configs, tag, False, precision, nve)
     assert a[4] == b[4] == 60
-    # the same float64 operations, compiled once by NVRTC (fused) and once by
-    # nvcc (separate kernel): agreement to rounding, amplified over 60 steps
-    assert np.max(np.abs(a[0] - b[0])) <= 1e-9
-    assert np.max(np.abs(a[1] - b[1])) <= 1e-8
-    assert np.max(np.abs(a[2] - b[2])) <= 1e-8
+    # the same operations, compiled once by NVRTC (fused) and once by nvcc
+    # (separate kernel); for small systems the fused step splits each
+    # particle's list over a warp, so its pair sums come in another order:
+    # agreement to rounding (float32 sums in the FP32 mode), amplified over 60
+    # steps
+    tol = 1e-9 if precision == "fp64" else 1e-6
+    assert np.max(np.abs(a[0] - b[0])) <= tol
+    assert np.max(np.abs(a[1] - b[1])) <= 10 * tol
+    assert np.max(np.abs(a[2] - b[2])) <= 10 * tol
     assert np.array_equal(a[3], b[3])
 
 
