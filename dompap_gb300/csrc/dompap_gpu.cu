@@ -20,6 +20,10 @@
 #include <cuda_runtime.h>
 #include <nvrtc.h>
 
+#include <dlfcn.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -755,10 +759,108 @@ struct PairLib {
 static std::mutex g_lib_mutex;
 static std::unordered_map<std::string, PairLib> g_libs;
 
+// --------------------------- on-disk cubin cache ------------------------
+// A pair program takes seconds to compile; its CUBIN is kept on disk under a
+// key of the program text and the NVRTC version, in DOMPAP_NVRTC_CACHE (empty
+// or "0": off) or else in _build/nvrtc_cache beside the library. A file holds
+// the program text it was compiled from and is used only when that text
+// matches exactly; unreadable or foreign files are ignored and rewritten.
+static std::string cubin_cache_dir(bool explicit_only) {
+    if (const char* env = std::getenv("DOMPAP_NVRTC_CACHE")) {
+        if (!*env || std::strcmp(env, "0") == 0) return "";
+        return env;
+    }
+    if (explicit_only) return "";
+    Dl_info info;
+    if (dladdr((void*)&cubin_cache_dir, &info) && info.dli_fname) {
+        const std::string lib = info.dli_fname;
+        const size_t k = lib.rfind('/');
+        if (k != std::string::npos) return lib.substr(0, k) + "/_build/nvrtc_cache";
+    }
+    return "";
+}
+
+static std::string cubin_cache_path(const std::string& dir, const std::string& src) {
+    uint64_t h = 1469598103934665603ull;  // FNV-1a
+    auto mix = [&h](const void* data, size_t len) {
+        const unsigned char* b = (const unsigned char*)data;
+        for (size_t i = 0; i < len; ++i) {
+            h ^= b[i];
+            h *= 1099511628211ull;
+        }
+    };
+    mix(src.data(), src.size());
+    int major = 0, minor = 0;
+    nvrtcVersion(&major, &minor);
+    mix(&major, sizeof(major));
+    mix(&minor, sizeof(minor));
+    char name[64];
+    snprintf(name, sizeof(name), "/%016llx.dpcubin", (unsigned long long)h);
+    return dir + name;
+}
+
+static const char kCacheMagic[8] = {'D', 'P', 'C', 'U', 'B', 'I', 'N', '1'};
+
+static bool cubin_cache_read(const std::string& path, const std::string& src, std::vector<char>* cubin) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) return false;
+    bool ok = false;
+    char magic[8];
+    uint64_t src_len = 0, bin_len = 0;
+    if (std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kCacheMagic, 8) == 0 &&
+        std::fread(&src_len, sizeof(src_len), 1, f) == 1 && src_len == src.size()) {
+        std::string text(src_len, '\0');
+        if (std::fread(&text[0], 1, src_len, f) == src_len && text == src &&
+            std::fread(&bin_len, sizeof(bin_len), 1, f) == 1 && bin_len > 0 && bin_len < (1ull << 30)) {
+            cubin->resize(bin_len);
+            ok = std::fread(cubin->data(), 1, bin_len, f) == bin_len;
+        }
+    }
+    std::fclose(f);
+    return ok;
+}
+
+static void cubin_cache_write(const std::string& dir, const std::string& path, const std::string& src,
+                              const std::vector<char>& cubin) {
+    // create the directory and its parent (the library's _build) if needed
+    const size_t k = dir.rfind('/');
+    if (k != std::string::npos && k > 0) mkdir(dir.substr(0, k).c_str(), 0755);
+    mkdir(dir.c_str(), 0755);
+    const std::string tmp = path + ".tmp" + std::to_string((long long)getpid());
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return;
+    const uint64_t src_len = src.size(), bin_len = cubin.size();
+    bool ok = std::fwrite(kCacheMagic, 1, 8, f) == 8 && std::fwrite(&src_len, sizeof(src_len), 1, f) == 1 &&
+              std::fwrite(src.data(), 1, src_len, f) == src_len && std::fwrite(&bin_len, sizeof(bin_len), 1, f) == 1 &&
+              std::fwrite(cubin.data(), 1, bin_len, f) == bin_len;
+    ok = (std::fclose(f) == 0) && ok;
+    if (ok)
+        std::rename(tmp.c_str(), path.c_str());  // atomic: readers see a whole file or none
+    else
+        std::remove(tmp.c_str());
+}
+
 // NVRTC: program text -> sm_103a CUBIN (host only; no GPU needed).
 // resource_log (optional): compile with the assembler's verbose report
 // (registers, spill bytes, shared memory per kernel) and return that log.
-static int nvrtc_cubin(const std::string& src, std::vector<char>* cubin, std::string* resource_log = nullptr) {
+static int nvrtc_compile(const std::string& src, std::vector<char>* cubin, std::string* resource_log);
+
+// cache: use the on-disk cubin cache (explicit_only: only when
+// DOMPAP_NVRTC_CACHE names a directory).
+static int nvrtc_cubin(const std::string& src, std::vector<char>* cubin, std::string* resource_log = nullptr,
+                       bool cache = false, bool explicit_only = false) {
+    const std::string dir = cache && !resource_log ? cubin_cache_dir(explicit_only) : std::string();
+    if (!dir.empty()) {
+        const std::string path = cubin_cache_path(dir, src);
+        if (cubin_cache_read(path, src, cubin)) return DP_OK;
+        RET(nvrtc_compile(src, cubin, nullptr));
+        cubin_cache_write(dir, path, src, *cubin);
+        return DP_OK;
+    }
+    return nvrtc_compile(src, cubin, resource_log);
+}
+
+static int nvrtc_compile(const std::string& src, std::vector<char>* cubin, std::string* resource_log) {
     nvrtcProgram prog;
     nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "dompap_pair.cu", 0, nullptr, nullptr);
     if (r != NVRTC_SUCCESS) return fail(DP_ERR_NVRTC, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
@@ -796,7 +898,7 @@ static int compile_pair_lib(const std::string& src, PairLib* out) {
         return DP_OK;
     }
     std::vector<char> cubin;
-    RET(nvrtc_cubin(src, &cubin));
+    RET(nvrtc_cubin(src, &cubin, nullptr, true));
     PairLib pl;
     CK(cudaLibraryLoadData(&pl.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
     CK(cudaLibraryGetKernel(&pl.forces, pl.lib, "dp_forces"));
@@ -3067,7 +3169,7 @@ static int nvrtc_check_impl(int dim, int precision, int pair_mode, int with_batc
     const std::string src = pair_program(dim, precision, pair_mode, one, one, device_source, with_batch != 0,
                                          step_blocks_for(dim, precision, pair_mode));
     std::vector<char> cubin;
-    RET(nvrtc_cubin(src, &cubin, resource_log));
+    RET(nvrtc_cubin(src, &cubin, resource_log, true, true));
     if (cubin_bytes) *cubin_bytes = (int64_t)cubin.size();
     return DP_OK;
 }

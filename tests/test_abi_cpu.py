@@ -158,3 +158,35 @@ def test_nvrtc_resource_report():
     assert {"dp_forces", "dp_step", "dp_energy", "dp_virial"} <= set(used)
     assert used["dp_step"] <= 64
     assert _registers_by_kernel(2)["dp_step"] <= 40
+
+
+def test_nvrtc_cubin_cache(tmp_path, monkeypatch):
+    """The on-disk cache of compiled pair programs: the first compile writes a
+    file keyed by the program text, the second reads it instead of compiling,
+    a damaged file is ignored and rewritten, another potential gets its own."""
+    import ctypes
+    import time
+
+    from dompap_gb300 import _lib, codegen
+
+    monkeypatch.setenv("DOMPAP_NVRTC_CACHE", str(tmp_path))
+    lib = _lib.load()
+    src, _ = codegen.make_pair_source("(1-r)**2", 1.0)
+
+    def compile_once(source):
+        size = ctypes.c_int64(0)
+        t0 = time.perf_counter()
+        assert lib.dp_nvrtc_check(3, 1, 0, 0, source.encode(), ctypes.byref(size)) == 0, lib.dp_last_error()
+        return size.value, time.perf_counter() - t0
+
+    size1, t_compile = compile_once(src)
+    files = sorted(tmp_path.glob("*.dpcubin"))
+    assert len(files) == 1 and files[0].read_bytes()[:8] == b"DPCUBIN1"
+    size2, t_cached = compile_once(src)
+    assert size2 == size1 and t_cached < 0.5 * t_compile
+    files[0].write_bytes(b"not a cubin")
+    size3, _ = compile_once(src)
+    assert size3 == size1 and files[0].read_bytes()[:8] == b"DPCUBIN1"
+    src_lj, _ = codegen.make_pair_source("4*(r**-12-r**-6)", 2.5)
+    compile_once(src_lj)
+    assert len(list(tmp_path.glob("*.dpcubin"))) == 2

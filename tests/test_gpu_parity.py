@@ -313,3 +313,33 @@ def test_run_host_equals_setters_run_getters(golden_configs):
         out.append((p_out, v_out, b_out))
     for a, b in zip(*out):
         assert np.array_equal(a, b)
+
+
+def test_cached_program_gives_the_same_forces(tmp_path):
+    """A pair program loaded from the on-disk cubin cache in a second process
+    gives bit-identical forces to the freshly compiled one."""
+    import os
+    import subprocess
+    import sys
+
+    script = (
+        "import sys, numpy as np; sys.path.insert(0, %r)\n"
+        "from dompap_gb300 import Simulation\n"
+        "from dompap_gb300.positions import FCC\n"
+        "sim = Simulation()\n"
+        "sim.set_positions(unit_cell_coordinates=FCC, cells=(4, 4, 4), lattice_constants=(1, 1, 1))\n"
+        "sim.set_masses(masses=1.0)\n"
+        "sim.set_density(density=0.9)\n"
+        "sim.positions = sim.positions + np.random.default_rng(1).normal(0, 0.03, sim.positions.shape)\n"
+        "sim.set_pair_potential('4*(r**-12-r**-6) + 0.1*exp(-r)', 2.2)\n"
+        "sim.set_neighbor_list(skin=0.3, max_number_of_neighbors=128)\n"
+        "np.save(sys.argv[1], sim.get_forces())\n"
+    ) % os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, DOMPAP_NVRTC_CACHE=str(tmp_path / "cache"))
+    outs = []
+    for k in range(2):
+        out = tmp_path / f"f{k}.npy"
+        subprocess.run([sys.executable, "-c", script, str(out)], env=env, check=True, timeout=600)
+        outs.append(np.load(out))
+    assert len(list((tmp_path / "cache").glob("*.dpcubin"))) >= 1
+    assert np.array_equal(outs[0], outs[1])
