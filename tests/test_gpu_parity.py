@@ -343,3 +343,32 @@ def test_cached_program_gives_the_same_forces(tmp_path):
         outs.append(np.load(out))
     assert len(list((tmp_path / "cache").glob("*.dpcubin"))) >= 1
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_overflow_during_run_replays_the_chunk():
+    """Particles converging on the box centre outgrow the list capacity inside
+    a run(): the chunk is restored from its backup, the capacity grows and the
+    chunk is replayed, ending bit-identical to a run that never overflowed."""
+    from dompap_gb300 import Simulation
+
+    def run(kmax):
+        sim = Simulation()
+        sim.set_positions(unit_cell_coordinates=([0.0, 0.0, 0.0],), cells=(8, 8, 8), lattice_constants=(1, 1, 1))
+        sim.set_masses(masses=1.0)
+        sim.set_density(density=1.0)
+        box = np.array(sim.box_vectors)
+        d = np.array(sim.positions) - 0.5 * box
+        sim.velocities = -3.0 * d  # everything heads for the centre
+        sim.set_pair_potential("(1-r)**2", 1.0)
+        sim.set_neighbor_list(skin=0.3, max_number_of_neighbors=kmax, method_str="cell list")
+        sim.set_integrator(time_step=0.005)
+        cap0 = int(sim._stats().neighbor_capacity)
+        sim.run_leap_frog(120)
+        st = sim._stats()
+        return np.array(sim.positions), np.array(sim.velocities), int(st.neighbor_capacity), cap0, int(st.steps)
+
+    pa, va, cap_a, cap0_a, steps_a = run(16)
+    pb, vb, cap_b, _, steps_b = run(2048)
+    assert steps_a == steps_b == 120
+    assert cap0_a == 16 and cap_a > 16  # grew inside the run
+    assert np.array_equal(pa, pb) and np.array_equal(va, vb)
