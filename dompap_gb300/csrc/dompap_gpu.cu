@@ -115,7 +115,6 @@ struct ShadowArgs {
     void* pos64;
     dp_dev_status* st;
     long long n;
-    double scale[DP_MAX_DIM];
     double scale64[DP_MAX_DIM];
     double box[DP_MAX_DIM];
 };
@@ -1112,7 +1111,6 @@ static int launch_shadow(dp_sim* s) {
     a.pos64 = s->pos64;
     a.st = s->dstat;
     a.n = s->n;
-    fill_scale(s, a.scale, nullptr);
     for (int k = 0; k < DP_MAX_DIM; ++k) a.scale64[k] = 18446744073709551616.0 / ((k < s->dim) ? s->box[k] : 1.0);
     for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
     CK(cudaMemsetAsync(&s->dstat->far, 0, sizeof(int32_t), s->stream));
