@@ -29,6 +29,9 @@ from .positions import FCC, generate_positions
 
 @dataclass
 class ReplicaSpec:
+    """One independent system of a batch: its lattice, velocities, box and
+    Langevin target temperature."""
+
     positions: np.ndarray   # (N, D), inside [0, L)
     velocities: np.ndarray  # (N, D)
     box: np.ndarray         # (D,)
@@ -36,6 +39,11 @@ class ReplicaSpec:
 
 
 class Replicas:
+    """Thousands of independent systems of one pair potential (uneven N and
+    temperature) advanced together by one persistent kernel per run; each
+    replica follows dompap's step (dompap/Simulation.py:681-737) with float32
+    pair forces and float64 integration."""
+
     def __init__(self, specs: list[ReplicaSpec], pair_potential_str: str, r_cut: float, time_step: float = 0.005,
                  damping_time: float = 0.1, mass: float = 1.0, seed: int | None = None, skin: float = 0.45,
                  max_number_of_neighbors: int = 0):
@@ -82,11 +90,15 @@ class Replicas:
         self.skin = skin
 
     def list_stats(self) -> dict:
+        """Verlet-list builds so far, replicas that overflowed their list (and
+        used the cell stencil), and the list capacity per particle."""
         b, o, k = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int32(0)
         _lib.check(_lib.load().dp_batch_list_stats(self._h, ctypes.byref(b), ctypes.byref(o), ctypes.byref(k)))
         return {"builds": int(b.value), "overflowed": int(o.value), "kmax": int(k.value)}
 
     def set_launch(self, split_n: int, threads_small: int, threads_large: int) -> None:
+        """Launch shape: replicas of up to ``split_n`` particles run in CTAs of
+        ``threads_small`` threads, larger ones in CTAs of ``threads_large``."""
         _lib.check(_lib.load().dp_batch_set_launch(self._h, int(split_n), int(threads_small), int(threads_large)))
         self.launch = (split_n, threads_small, threads_large)
 
@@ -118,6 +130,7 @@ class Replicas:
 
     # ---------------------------------------------------------------- results
     def state(self):
+        """(positions, velocities, images) of all replicas, (N_total, D) each."""
         pos = np.empty((self.ntot, self.dim))
         vel = np.empty((self.ntot, self.dim))
         img = np.empty((self.ntot, self.dim), dtype=np.int32)
@@ -125,9 +138,11 @@ class Replicas:
         return pos, vel, img
 
     def replica_slice(self, r: int) -> slice:
+        """Rows of replica ``r`` in the arrays of ``state()``."""
         return slice(int(self.offsets[r]), int(self.offsets[r + 1]))
 
     def last_forces(self) -> np.ndarray:
+        """float32 pair forces of the last step of a ``run(..., record_forces=True)``."""
         out = np.empty((self.ntot, self.dim))
         _lib.check(_lib.load().dp_batch_last_forces(self._h, _lib.dptr(out)))
         return out

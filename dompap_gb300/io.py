@@ -27,6 +27,8 @@ def _toml_value(value):
 
 
 def to_disk(sim, particle_data="simulation.csv", meta_data="simulation.toml") -> None:
+    """Particle CSV and TOML metadata as dompap writes them
+    (dompap/Simulation.py:1019-1079); the CSV is byte-identical."""
     dims = sim.get_dimensions_of_space()
     types = sim.particle_types
     masses = sim.masses
@@ -78,6 +80,8 @@ def to_disk(sim, particle_data="simulation.csv", meta_data="simulation.toml") ->
 
 def from_disk(sim, particle_data="simulation.csv", meta_data="simulation.toml", verbose=False,
               set_only_particle_data=False) -> dict:
+    """Read dompap's checkpoint files (dompap/Simulation.py:1081-1203) into
+    ``sim``; returns the metadata."""
     if not os.path.isfile(particle_data):
         raise FileNotFoundError(f"File not found: {particle_data}")
     if not os.path.isfile(meta_data):

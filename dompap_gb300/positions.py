@@ -10,6 +10,8 @@ import numpy as np
 
 
 def generate_positions(unit_cell_coordinates, cells, lattice_constants) -> np.ndarray:
+    """Lattice positions, cells in row-major order and the unit cell's sites
+    within each (dompap/positions.py:33-52)."""
     unit = np.asarray(unit_cell_coordinates, dtype=np.float64)
     cells = np.asarray(cells, dtype=np.int64)
     lat = np.asarray(lattice_constants, dtype=np.float64)

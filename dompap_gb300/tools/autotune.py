@@ -16,6 +16,8 @@ from time import perf_counter
 
 def autotune(sim, steps=100, test_double_loop=True, smallest_skin=0.1, step_skin=0.1, verbose=False,
              plot=False):
+    """Return ``sim`` with the fastest neighbour-list method and skin set
+    (dompap/tools/autotune.py:4-178; the procedure is the module docstring's)."""
     sim_copy = sim.copy()
     sim_copy.step()
     results = {}

@@ -77,3 +77,21 @@ def test_run_test_simulation():
     sim = run_test_simulation()
     assert sim.number_of_steps >= 1000
     assert np.isfinite(sim.get_potential_energy())
+
+
+def test_progress_bar_marks(capsys):
+    """tools.progress_bar (dompap/tools/progress_bar.py:1-21): dompap's
+    signature and marks — time and count every 50 strides, '|' every 10, ':'
+    every 5, '.' otherwise, the percentage overwritten in place, 'done'."""
+    import re
+
+    from dompap_gb300.tools import progress_bar
+
+    for step in range(0, 60, 1):
+        progress_bar(step, 100, 1)
+    progress_bar(100, 100, 1, finalize=True)
+    out = re.sub(r"\d{4}-\d\d-\d\d \d\d:\d\d:\d\d(\.\d+)?", "T", capsys.readouterr().out)
+    marks = re.sub(r"\x08{7}| +\d+\.\d%", "", out)
+    assert marks.startswith("T            0 |....:....|....:....|")
+    assert "|\nT           50 |....:....  done" in marks
+    assert marks.endswith("  done\n")
