@@ -4,7 +4,6 @@ the host by evaluating the printed expressions with Python semantics."""
 import math
 import re
 
-import numpy as np
 import pytest
 import sympy as sp
 
