@@ -75,3 +75,20 @@ def test_constants_and_horner_form():
 def test_rejects_foreign_symbols():
     with pytest.raises(ValueError):
         codegen.make_pair_source("r**2 + a", 1.0)
+
+
+def test_surrogate_split_of_a_potential():
+    """The surrogate learns only the costly terms (exp, cos, non-integer
+    powers); the cheap ones stay generated code, and the two add up to the
+    potential."""
+    from dompap_gb300.mlp import split_costly
+
+    pot = "4*(r**-12-r**-6) + 0.5*exp(-(r-1.5)**2/0.02) + 0.1*cos(4*r)*exp(-r) - 0.25 - (r - 3.0)*0.125"
+    cheap, costly = split_costly(pot)
+    r = sp.Symbol("r")
+    assert sp.simplify(sp.sympify(cheap) + sp.sympify(costly) - sp.sympify(pot)) == 0
+    assert not sp.sympify(cheap).has(sp.exp, sp.cos)
+    assert sp.sympify(costly).has(sp.exp) and sp.sympify(costly).has(sp.cos)
+    assert sp.sympify(costly).free_symbols == {r}
+    cheap2, costly2 = split_costly("r**0.5 + r**-6")
+    assert sp.sympify(costly2) == sp.sympify("r**0.5") and sp.sympify(cheap2) == sp.sympify("r**-6")
