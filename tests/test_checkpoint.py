@@ -95,3 +95,29 @@ def test_restored_system_reproduces_reference_observables(tmp_path):
     out_csv, out_toml = tmp_path / "c.csv", tmp_path / "c.toml"
     sim.to_disk(particle_data=str(out_csv), meta_data=str(out_toml))
     assert out_csv.read_bytes() == open(CSV, "rb").read()
+
+
+@pytest.mark.parametrize("dim", [3, 4])
+def test_round_trip_other_dimensions(tmp_path, dim):
+    """to_disk -> from_disk restores positions, images, velocities, betas,
+    types and masses exactly in 3 and 4 dimensions (the format's columns
+    follow the dimension, dompap/Simulation.py:1019-1203)."""
+    from dompap_gb300 import io
+
+    rng = np.random.default_rng(dim)
+    n = 17
+    meta = _reference_meta()
+    st = _HostState(meta)
+    st.positions = rng.uniform(0.0, 5.0, size=(n, dim))
+    st.image_positions = rng.integers(-4, 5, size=(n, dim)).astype(np.int32)
+    st.velocities = rng.normal(size=(n, dim))
+    st.betas = rng.normal(scale=0.1, size=(n, dim))
+    st.particle_types = rng.integers(0, 3, size=(n, 1)).astype(np.int32)
+    st.masses = rng.uniform(0.5, 2.0, size=(n, 1))
+    st.box_vectors = np.full(dim, 5.0)
+    csv, toml = tmp_path / "s.csv", tmp_path / "s.toml"
+    io.to_disk(st, particle_data=str(csv), meta_data=str(toml))
+    back = _HostState(meta)
+    io.from_disk(back, particle_data=str(csv), meta_data=str(toml), set_only_particle_data=True)
+    for name in ("positions", "image_positions", "velocities", "betas", "particle_types", "masses"):
+        assert np.array_equal(np.asarray(getattr(back, name)).reshape(getattr(st, name).shape), getattr(st, name)), name
