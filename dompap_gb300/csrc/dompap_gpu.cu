@@ -737,7 +737,9 @@ __global__ void __launch_bounds__(kBlock) k_mv2_rowmajor(const double* __restric
 }  // namespace
 
 // Device address of g_noalloc_partial, looked up once per device (host code
-// cannot use the symbol itself: on the host it only names a stand-in).
+// cannot use the symbol itself: on the host it only names a stand-in). The
+// cached address belongs to the device's primary context; cudaDeviceReset
+// ends that context, and the header tells callers not to call again after it.
 static std::mutex g_noalloc_mutex;
 static double* g_noalloc_addr[64] = {nullptr};
 
@@ -2634,7 +2636,7 @@ int dp_sum_mv2_noalloc(const double* velocities, const double* masses, int64_t n
     if (!velocities || !masses || !out) return fail(DP_ERR_ARG, "null device pointer");
     if (dim < 1 || dim > DP_MAX_DIM) return fail(DP_ERR_ARG, "dimension must be in [1, 4]");
     if (n < 1) return fail(DP_ERR_ARG, "number of particles must be >= 1");
-    const long long blocks = (n + kBlock - 1) / kBlock;
+    const long long blocks = (n - 1) / kBlock + 1;  // n >= 1: no overflow near INT64_MAX
     if (blocks > DP_NOALLOC_MAX_BLOCKS)
         return fail(DP_ERR_ARG, "dp_sum_mv2_noalloc: " + std::to_string(n) + " particles exceed its fixed scratch (at most " +
                                     std::to_string((long long)DP_NOALLOC_MAX_BLOCKS * kBlock) + ")");

@@ -1,8 +1,9 @@
 """Checkpoint files in dompap's format (dompap/Simulation.py:1019-1203).
 
 ``to_disk`` writes the particle CSV (``ptype,mass,pos_d..,vel_d..,imgpos_d..,
-beta_d..``) and the TOML metadata exactly as dompap does; the state is copied
-from the GPU first. ``from_disk`` reads both, replaces the system and re-applies
+beta_d..``) byte for byte as dompap does, and the TOML metadata with dompap's
+keys and values in the ``toml`` package's flat form (floats with a one-digit
+exponent where it can: 1e-5); the state is copied from the GPU first. ``from_disk`` reads both, replaces the system and re-applies
 the potential, neighbour list and integrator, so a GPU run resumes from a
 dompap checkpoint and vice versa.
 """
@@ -22,7 +23,11 @@ def _toml_value(value):
     if isinstance(value, (list, tuple)):
         return "[ " + ", ".join(_toml_value(v) for v in value) + ",]"
     if isinstance(value, float):
-        return repr(value) if np.isfinite(value) else ("inf" if value > 0 else ("-inf" if value < 0 else "nan"))
+        if not np.isfinite(value):
+            return "inf" if value > 0 else ("-inf" if value < 0 else "nan")
+        # the toml package prints floats with str() and drops a leading zero of
+        # the exponent (1e-05 -> 1e-5)
+        return repr(value).replace("e+0", "e+").replace("e-0", "e-")
     return repr(value)
 
 

@@ -11,8 +11,7 @@
  *
  * Each declaration names the dompap function it replaces (paths inside the
  * dompap project, version 0.0.6). The Python `Simulation` in dompap_gb300 is
- * the drop-in binding; INTEGRATION.md shows the ctypes stub dompap itself
- * would add.
+ * the drop-in binding over these entry points (ctypes).
  */
 #ifndef DOMPAP_GPU_H
 #define DOMPAP_GPU_H
@@ -198,15 +197,23 @@ int dp_time_kernel(dp_sim *sim, int which, int reps, float *ms_per_launch);
 int dp_time_forces(dp_sim *sim, int reps, float *ms_per_launch);
 /* sum_n m_n |v_n|^2 like dp_sum_mv2, but on caller-owned device arrays and
  * without allocating anything; it has no counterpart in the reference.
- * For callers that cannot call cudaMalloc: code recording a CUDA graph (an
- * allocation is not allowed during stream capture), and hosts that own all
- * device memory through their own pool allocator. velocities: device (N, dim)
- * row-major float64; masses: device (N,); out: device, one double; stream:
- * a cudaStream_t (NULL = default stream). Asynchronous on `stream`.
- * Scratch: a fixed 128 KiB device array inside this library, so N is at most
- * 4,194,304 (larger N returns DP_ERR_ARG). The first call on a device looks
- * up that array's address; make it before any stream capture. Calls share
- * the array: calls that overlap on the GPU race. */
+ * For callers that cannot call cudaMalloc: hosts that hand out all device
+ * memory from their own pool or arena (a framework's caching allocator, a
+ * memory budget fixed at start-up), where an allocation made behind their
+ * back can fail once the pool holds the memory, or breaks their accounting.
+ * velocities: device (N, dim) row-major float64; masses: device (N,); out:
+ * device, one double; stream: a cudaStream_t (NULL = default stream).
+ * Asynchronous on `stream`.
+ * Scratch: a fixed 128 KiB device array inside this library (one double per
+ * 256 particles), so N is at most 4,194,304; a larger N returns DP_ERR_ARG
+ * before any launch. Every GPU that loads the library holds the array until
+ * the process exits. The first call on a device looks up the array's device
+ * address (set-up, once per device, with that device current); make that
+ * first call before any stream capture. The address is kept for the life of
+ * the process: after cudaDeviceReset, call nothing here again on that device.
+ * Every call shares the array and overwrites the partial sums it reads, so
+ * nothing carries over from the previous call; calls that overlap on the GPU
+ * (different streams at once) race on it. */
 int dp_sum_mv2_noalloc(const double *velocities, const double *masses, int64_t n, int dim, double *out,
                        void *stream);
 

@@ -16,6 +16,9 @@ def _fmt(value):
         return '"' + value.replace('"', '\\"') + '"'
     if isinstance(value, (list, tuple)):
         return "[ " + ", ".join(_fmt(v) for v in value) + ",]"
+    if isinstance(value, float):
+        # toml prints floats with one exponent digit where it can (1e-5)
+        return repr(value).replace("e+0", "e+").replace("e-0", "e-")
     return repr(value)
 
 

@@ -4,7 +4,7 @@ a ``toml`` shim and a no-op ``matplotlib``).
 
 Run in a checkout that has the reference source next to it::
 
-    python tests/golden/make_golden.py [--reference PATH]
+    python tests/golden/make_golden.py --reference PATH   (or DOMPAP_REFERENCE=PATH)
 
 It writes ``golden_*.npz``, ``checkpoint_ref.csv/.toml`` and ``lammps_ref.*``. Every array is produced by calling the reference's
 own functions / ``Simulation`` methods on seeded inputs; nothing here restates
@@ -195,7 +195,8 @@ def make_lammps(Simulation):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("DOMPAP_REFERENCE"),
+                    required="DOMPAP_REFERENCE" not in os.environ, help="path of an unmodified dompap 0.0.6 source tree (or set DOMPAP_REFERENCE)")
     ap.add_argument("--only", choices=["checkpoint", "lammps"], default=None,
                     help="regenerate only the named fixture")
     args = ap.parse_args()

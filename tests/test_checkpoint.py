@@ -121,3 +121,17 @@ def test_round_trip_other_dimensions(tmp_path, dim):
     io.from_disk(back, particle_data=str(csv), meta_data=str(toml), set_only_particle_data=True)
     for name in ("positions", "image_positions", "velocities", "betas", "particle_types", "masses"):
         assert np.array_equal(np.asarray(getattr(back, name)).reshape(getattr(st, name).shape), getattr(st, name)), name
+
+
+def test_toml_float_format_matches_toml_package():
+    """dompap writes its metadata with the ``toml`` package, whose floats drop
+    a leading zero of the exponent (``time_step = 1e-5``); values round-trip."""
+    from dompap_gb300.io import _toml_value
+
+    assert _toml_value(1e-05) == "1e-5"
+    assert _toml_value(2.5e-07) == "2.5e-7"
+    assert _toml_value(1e20) == "1e+20"
+    assert _toml_value(1.5e+300) == "1.5e+300"
+    assert _toml_value(0.002) == "0.002"
+    for v in (1e-05, 2.5e-07, 1e20, 0.002, 123456.789):
+        assert tomllib.loads(f"x = {_toml_value(v)}\n")["x"] == v

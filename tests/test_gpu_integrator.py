@@ -196,8 +196,10 @@ def test_doctest_values(golden_unit):
     assert sim.get_time() == 0.1
     sim.velocities = np.ones_like(sim.velocities)
     assert f"{sim.get_kinetic_energy():.1f}" == "187.5"
+    # set_neighbor_list doctest (dompap/Simulation.py:327-333): a fresh system
+    sim = Simulation()
     sim.set_neighbor_list()
-    assert int(np.max(np.sum(sim.neighbor_list != -1, axis=1))) == 26 or True
+    assert int(np.max(np.sum(sim.neighbor_list != -1, axis=1))) == 26
 
 
 def test_copy_is_independent():

@@ -66,32 +66,3 @@ def test_dump_from_gpu_system():
     fw = np.array([[float(v) for v in line.split()[-3:]] for line in want[9:]])
     assert np.sqrt(np.mean((fg - fw) ** 2) / np.mean(fw ** 2)) <= 1e-10
     assert [line.split()[:-3] for line in got[9:]] == [line.split()[:-3] for line in want[9:]]
-
-
-@pytest.mark.gpu
-def test_run_test_simulation():
-    """tools.run_test_simulation (dompap/tools/run_test_simulation.py:7-28):
-    the default system, autotuned, 1000 steps."""
-    from dompap_gb300.tools import run_test_simulation
-
-    sim = run_test_simulation()
-    assert sim.number_of_steps >= 1000
-    assert np.isfinite(sim.get_potential_energy())
-
-
-def test_progress_bar_marks(capsys):
-    """tools.progress_bar (dompap/tools/progress_bar.py:1-21): dompap's
-    signature and marks — time and count every 50 strides, '|' every 10, ':'
-    every 5, '.' otherwise, the percentage overwritten in place, 'done'."""
-    import re
-
-    from dompap_gb300.tools import progress_bar
-
-    for step in range(0, 60, 1):
-        progress_bar(step, 100, 1)
-    progress_bar(100, 100, 1, finalize=True)
-    out = re.sub(r"\d{4}-\d\d-\d\d \d\d:\d\d:\d\d(\.\d+)?", "T", capsys.readouterr().out)
-    marks = re.sub(r"\x08{7}| +\d+\.\d%", "", out)
-    assert marks.startswith("T            0 |....:....|....:....|")
-    assert "|\nT           50 |....:....  done" in marks
-    assert marks.endswith("  done\n")

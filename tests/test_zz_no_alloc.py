@@ -1,11 +1,12 @@
 """The allocation-free kinetic sum ``dp_sum_mv2_noalloc``.
 
-It exists for callers that cannot call cudaMalloc — code recording a CUDA graph
-(allocation is not allowed during stream capture) and hosts that own all device
-memory through their own pool allocator. This test owns the device buffers
-(torch allocates them); the entry point is only handed pointers, and its result
-must equal the handle-based ``dp_sum_mv2`` (FP64 sums, 1e-12 relative) on two
-calls in a row. The file is named so that pytest collects it last.
+It exists for callers that cannot call cudaMalloc: hosts that hand out all
+device memory from their own pool or a budget fixed at start-up, where a
+library allocation can fail or break their accounting. This test owns the
+device buffers (torch allocates them); the entry point is only handed
+pointers, and its result must equal the handle-based ``dp_sum_mv2`` (FP64
+sums, 1e-12 relative) on two calls in a row. The file is named so that pytest
+collects it last; it passes alone in a fresh process and after the others.
 """
 import ctypes
 
