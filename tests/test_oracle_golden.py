@@ -214,3 +214,19 @@ def test_gjf_tau_inf_trajectory(golden_traj):
     close(sys_.positions, t["positions"], 1.0)
     close(sys_.velocities, t["velocities"], 1.0)
     assert np.array_equal(sys_.images, t["images"])
+
+
+def test_rdf_per_type_pair():
+    """g(r) of each type pair of the binary configuration: the oracle on the
+    type subsets equals the reference's own get_radial_distribution_function
+    (dompap/positions.py:58-87) called on the same subsets."""
+    from conftest import load_golden
+
+    gold = load_golden("golden_rdf_types.npz")
+    cfg = load_golden("golden_configs.npz")
+    pos, box = cfg["wahn/positions"], cfg["wahn/box"]
+    types = cfg["wahn/types"].reshape(-1)
+    for a, b, key in ((0, 0, "AA"), (0, 1, "AB"), (1, 1, "BB")):
+        r, g = ref.radial_distribution_function(pos[types == a], pos[types == b], box, gold["bins"])
+        assert np.array_equal(r, gold[f"{key}/r"])
+        np.testing.assert_allclose(g, gold[f"{key}/g"], rtol=1e-13, atol=0)
