@@ -77,36 +77,28 @@ namespace {
 
 constexpr int kBlock = 256;
 
-__global__ void k_aos_to_soa_f64(const double* __restrict__ in, double* __restrict__ out, long long n, int dim) {
+// Host layout (particle id major, (n, dim)) <-> device SoA in slot order:
+// element (id, k) lives at k * n + slot_of[id] (slot_of null: slot = id). The
+// host side is read or written contiguously (it may be page-locked host memory
+// read over the host link); the scattered side is device memory.
+template <typename T>
+__global__ void k_host_to_slots(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict__ slot_of,
+                                long long n, int dim) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n * dim) return;
     const long long i = t / dim;
     const int k = (int)(t - i * dim);
-    out[k * n + i] = in[t];
+    out[k * n + (slot_of ? slot_of[i] : i)] = in[t];
 }
 
-__global__ void k_soa_to_aos_f64(const double* __restrict__ in, double* __restrict__ out, long long n, int dim) {
+template <typename T>
+__global__ void k_slots_to_host(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict__ slot_of,
+                                long long n, int dim) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n * dim) return;
     const long long i = t / dim;
     const int k = (int)(t - i * dim);
-    out[t] = in[k * n + i];
-}
-
-__global__ void k_aos_to_soa_i32(const int32_t* __restrict__ in, int32_t* __restrict__ out, long long n, int dim) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n * dim) return;
-    const long long i = t / dim;
-    const int k = (int)(t - i * dim);
-    out[k * n + i] = in[t];
-}
-
-__global__ void k_soa_to_aos_i32(const int32_t* __restrict__ in, int32_t* __restrict__ out, long long n, int dim) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n * dim) return;
-    const long long i = t / dim;
-    const int k = (int)(t - i * dim);
-    out[t] = in[k * n + i];
+    out[t] = in[k * n + (slot_of ? slot_of[i] : i)];
 }
 
 struct ShadowArgs {
@@ -192,90 +184,292 @@ __global__ void k_skin_check(SkinArgs a) {
     if (__any_sync(0xffffffffu, old) && (threadIdx.x & 31) == 0) atomicExch(&a.st->need_rebuild, 1);
 }
 
-// --------------------------- cell list ------------------------------------
-// Cells are at least `cutoff` wide (nc = floor(L / cutoff) per axis, >= 3), so
-// every pair closer than the cutoff sits in the 3^D stencil of its cell. This
-// is the cell list of dompap/neighbor_list.py:42-180 made exact: the
-// reference uses cells of width `cutoff` with nc = ceil(L / cutoff) and misses
-// pairs when L / cutoff is not an integer.
-struct CellArgs {
-    const double* pos;
-    int32_t* cell_cnt;
-    int32_t* cell_mem;
+// --------------------------- cell binning ---------------------------------
+// The cell list of dompap/neighbor_list.py:42-180 as a counting sort. Cells
+// are at least `cutoff` wide plus an absolute margin for the rounding of the
+// fixed-point shadows (nc = floor(L / w) per axis, >= 3), so every pair
+// closer than the cutoff lies in the 3^D stencil of its cell; the reference
+// uses cells of width `cutoff` with nc = ceil(L / cutoff) and misses pairs
+// when L / cutoff is not an integer. A particle's cell comes from its shadow
+// in integer arithmetic, c_k = (u_k nc_k) >> 32, i.e. from its periodic image
+// in [0, L). Cells are keyed in Morton (Z) order of their coordinates
+// (row-major when the padded Morton range would be too large), counted,
+// prefix-summed into contiguous slot ranges, and each particle is given a
+// slot in its cell's range, ties ordered by particle id, so that the order is
+// a function of the positions alone. The per-particle state then moves into
+// that order (k_permute): the partners a step gathers lie close together in
+// memory, and each cell of the Verlet build is one contiguous range.
+struct BinArgs {
+    const void* shadow;    // shadows of the current slots
+    const int32_t* order;  // particle id of each current slot
+    int32_t* key;          // [n] cell key of each current slot
+    int32_t* rank;         // [n] arrival rank within its cell (atomic)
+    int32_t* bin_cnt;      // [nbins] particles per cell key
+    int32_t* bin_start;    // [nbins + 1] first slot of each cell key
+    int32_t* bin_part;     // [ceil(nbins / kScanTile)] scan partial sums
+    int32_t* src_of;       // [n] current slot of the particle that new slot t receives
     dp_dev_status* st;
     long long n;
-    long long ncell;
-    int ccap;
+    long long nbins;
     int nc[DP_MAX_DIM];
-    double inv_w[DP_MAX_DIM];
-    double box[DP_MAX_DIM];
+    int morton;            // 1: Morton keys on the power-of-two padded grid
 };
 
-// Cell of a position, binned on its periodic image in [0, L) so that positions
-// the user left outside the box are still found; the exact pair test then uses
-// the raw coordinates with the reference's single-shift rule.
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 4;
+constexpr int kScanTile = kScanThreads * kScanPer;
+
+// Bit interleaving for Morton keys: bit b of x moves to bit D b.
 template <int D>
-__device__ __forceinline__ void cell_coords(const double* x, const int* nc, const double* inv_w, const double* box,
-                                            int* c) {
+__device__ __forceinline__ uint32_t dp_spread_bits(uint32_t x);
+template <>
+__device__ __forceinline__ uint32_t dp_spread_bits<2>(uint32_t x) {
+    x &= 0xFFFFu;
+    x = (x | (x << 8)) & 0x00FF00FFu;
+    x = (x | (x << 4)) & 0x0F0F0F0Fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    return (x | (x << 1)) & 0x55555555u;
+}
+template <>
+__device__ __forceinline__ uint32_t dp_spread_bits<3>(uint32_t x) {
+    x &= 0x3FFu;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    return (x | (x << 2)) & 0x09249249u;
+}
+template <>
+__device__ __forceinline__ uint32_t dp_spread_bits<4>(uint32_t x) {
+    x &= 0xFFu;
+    x = (x | (x << 12)) & 0x000F000Fu;
+    x = (x | (x << 6)) & 0x03030303u;
+    return (x | (x << 3)) & 0x11111111u;
+}
+
+// Cell coordinates of a shadow (fixed-point position in [0, 2^32) per axis).
+template <int D>
+__device__ __forceinline__ void shadow_cell(const uint32_t* u, const int* nc, int* c) {
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
-        double xw = x[k];
-        if (!(xw >= 0.0 && xw < box[k])) xw -= floor(xw / box[k]) * box[k];
-        const double t = floor(xw * inv_w[k]);
-        int ck = (t >= 0.0) ? (int)fmin(t, (double)(nc[k] - 1)) : 0;  // NaN -> 0
-        c[k] = ck;
-    }
+    for (int k = 0; k < D; ++k) c[k] = (int)(((unsigned long long)u[k] * (unsigned)nc[k]) >> 32);
 }
 
 template <int D>
-__device__ __forceinline__ long long cell_linear(const int* c, const int* nc) {
-    long long l = c[0];
+__device__ __forceinline__ int cell_key(const int* c, const int* nc, int morton) {
+    if (morton) {
+        uint32_t key = 0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) key |= dp_spread_bits<D>((uint32_t)c[k]) << (D - 1 - k);
+        return (int)key;
+    }
+    int l = c[0];
 #pragma unroll
     for (int k = 1; k < D; ++k) l = l * nc[k] + c[k];
     return l;
 }
 
-__global__ void k_cell_clear(CellArgs a) {
+__global__ void k_bin_clear(BinArgs a) {
     if (!a.st->need_rebuild) return;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < a.ncell;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < a.nbins;
          c += (long long)gridDim.x * blockDim.x)
-        a.cell_cnt[c] = 0;
+        a.bin_cnt[c] = 0;
 }
 
 template <int D>
-__global__ void k_cell_fill(CellArgs a) {
+__global__ void k_bin_count(BinArgs a) {
     if (!a.st->need_rebuild) return;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    double x[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) x[k] = a.pos[k * a.n + i];
+    typedef typename dp_shadow_t<D>::type sh_t;
+    uint32_t u[D];
+    dp_shadow_unpack<D>(((const sh_t*)a.shadow)[i], u);
     int c[D];
-    cell_coords<D>(x, a.nc, a.inv_w, a.box, c);
-    const long long l = cell_linear<D>(c, a.nc);
-    const int slot = atomicAdd(a.cell_cnt + l, 1);
-    if (slot < a.ccap)
-        a.cell_mem[l * a.ccap + slot] = (int32_t)i;
-    else
-        atomicMax(&a.st->cell_overflow, slot + 1);
+    shadow_cell<D>(u, a.nc, c);
+    const int key = cell_key<D>(c, a.nc, a.morton);
+    a.key[i] = key;
+    a.rank[i] = atomicAdd(a.bin_cnt + key, 1);
 }
 
-// Sort each cell's members by index so the Verlet rows are deterministic.
-__global__ void k_cell_sort(CellArgs a) {
+// Exclusive scan of one value per thread over a block of kScanThreads.
+__device__ __forceinline__ int block_exclusive_scan(int v, int* smem, int* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) smem[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < nwarps ? smem[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        smem[lane] = w;
+    }
+    __syncthreads();
+    const int before = warp ? smem[warp - 1] : 0;
+    *total = smem[nwarps - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+// Scan of the cell counts: per-tile sums, a one-block scan of those, then
+// each tile's exclusive scan plus its offset (bin_start[nbins] = n).
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(BinArgs a) {
     if (!a.st->need_rebuild) return;
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= a.ncell) return;
-    const int m = min(a.cell_cnt[c], a.ccap);
-    int32_t* mem = a.cell_mem + c * a.ccap;
-    for (int t = 1; t < m; ++t) {
-        const int32_t v = mem[t];
+    __shared__ int smem[32];
+    const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanPer;
+    int v = 0;
+#pragma unroll
+    for (int t = 0; t < kScanPer; ++t)
+        if (base + t < a.nbins) v += a.bin_cnt[base + t];
+    int total = 0;
+    block_exclusive_scan(v, smem, &total);
+    if (threadIdx.x == 0) a.bin_part[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_top(BinArgs a, int parts) {
+    if (!a.st->need_rebuild) return;
+    __shared__ int smem[32];
+    const int per = (parts + kScanThreads - 1) / kScanThreads;
+    const int b = threadIdx.x * per;
+    int v = 0;
+    for (int t = 0; t < per; ++t)
+        if (b + t < parts) v += a.bin_part[b + t];
+    int total = 0;
+    int run = block_exclusive_scan(v, smem, &total);
+    for (int t = 0; t < per; ++t)
+        if (b + t < parts) {
+            const int x = a.bin_part[b + t];
+            a.bin_part[b + t] = run;
+            run += x;
+        }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_down(BinArgs a) {
+    if (!a.st->need_rebuild) return;
+    __shared__ int smem[32];
+    const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanPer;
+    int c[kScanPer];
+    int v = 0;
+#pragma unroll
+    for (int t = 0; t < kScanPer; ++t) {
+        c[t] = base + t < a.nbins ? a.bin_cnt[base + t] : 0;
+        v += c[t];
+    }
+    int total = 0;
+    int run = a.bin_part[blockIdx.x] + block_exclusive_scan(v, smem, &total);
+#pragma unroll
+    for (int t = 0; t < kScanPer; ++t)
+        if (base + t < a.nbins) {
+            a.bin_start[base + t] = run;
+            run += c[t];
+        }
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.bin_start[a.nbins] = (int)a.n;
+}
+
+__global__ void k_bin_scatter(BinArgs a) {
+    if (!a.st->need_rebuild) return;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    a.src_of[a.bin_start[a.key[i]] + a.rank[i]] = (int32_t)i;
+}
+
+// Each cell's range ordered by particle id (the atomic ranks are not
+// deterministic; the result is).
+__global__ void k_bin_sort(BinArgs a) {
+    if (!a.st->need_rebuild) return;
+    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= a.nbins) return;
+    const int lo = a.bin_start[b], hi = a.bin_start[b + 1];
+    for (int t = lo + 1; t < hi; ++t) {
+        const int32_t v = a.src_of[t];
+        const int32_t id = a.order[v];
         int u = t - 1;
-        while (u >= 0 && mem[u] > v) {
-            mem[u + 1] = mem[u];
+        while (u >= lo && a.order[a.src_of[u]] > id) {
+            a.src_of[u + 1] = a.src_of[u];
             --u;
         }
-        mem[u + 1] = v;
+        a.src_of[u + 1] = v;
     }
+}
+
+// --------------------------- permutation of the state ----------------------
+// Arrays that move with their particle: element `esize` bytes, `comps`
+// components at a stride of n elements (SoA), or one vector per particle.
+struct PermArray {
+    void* data;     // the state array
+    void* scratch;  // same shape, receives the permuted copy
+    int esize;      // 1, 4, 8, 16 or 32
+    int comps;
+};
+
+constexpr int kMaxPermArrays = 12;
+
+struct PermArgs {
+    PermArray arr[kMaxPermArrays];
+    int count;
+    const int32_t* src_of;  // new slot t <- current slot src_of[t] (null: copy back)
+    const int32_t* order;   // particle id of each current slot
+    int32_t* slot_of;       // [n] slot of each particle id (updated)
+    dp_dev_status* st;
+    long long n;
+};
+
+__device__ __forceinline__ void copy_elem(const void* src, void* dst, long long from, long long to, int esize) {
+    switch (esize) {
+        case 1: ((uint8_t*)dst)[to] = ((const uint8_t*)src)[from]; break;
+        case 4: ((uint32_t*)dst)[to] = ((const uint32_t*)src)[from]; break;
+        case 8: ((uint2*)dst)[to] = ((const uint2*)src)[from]; break;
+        case 16: ((uint4*)dst)[to] = ((const uint4*)src)[from]; break;
+        default:
+            ((uint4*)dst)[2 * to] = ((const uint4*)src)[2 * from];
+            ((uint4*)dst)[2 * to + 1] = ((const uint4*)src)[2 * from + 1];
+            break;
+    }
+}
+
+// Gather every state array into cell order (into the scratch arrays) and
+// record the new slot of each particle id.
+__global__ void k_permute(PermArgs p) {
+    if (!p.st->need_rebuild) return;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.n) return;
+    const long long o = p.src_of[t];
+    for (int q = 0; q < p.count; ++q) {
+        const PermArray& a = p.arr[q];
+        for (int k = 0; k < a.comps; ++k) copy_elem(a.data, a.scratch, k * p.n + o, k * p.n + t, a.esize);
+    }
+    p.slot_of[p.order[o]] = (int32_t)t;
+}
+
+// The permuted copies back into the state arrays (the kernels captured after
+// a rebuild read the state at fixed addresses).
+__global__ void k_permute_back(PermArgs p) {
+    if (!p.st->need_rebuild) return;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.n) return;
+    for (int q = 0; q < p.count; ++q) {
+        const PermArray& a = p.arr[q];
+        for (int k = 0; k < a.comps; ++k) copy_elem(a.scratch, a.data, k * p.n + t, k * p.n + t, a.esize);
+    }
+}
+
+__global__ void k_iota(int32_t* a, int32_t* b, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    a[i] = (int32_t)i;
+    b[i] = (int32_t)i;
+}
+
+// slot_of from order (after a restore of the backed-up order).
+__global__ void k_invert_order(const int32_t* order, int32_t* slot_of, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    slot_of[order[i]] = (int32_t)i;
 }
 
 // --------------------------- Verlet list ----------------------------------
@@ -289,14 +483,13 @@ struct NlArgs {
     void* shadow_ref;
     int32_t* nl;
     int32_t* cnt;
-    const int32_t* cell_cnt;
-    const int32_t* cell_mem;
+    const int32_t* bin_start;  // cell ranges of the cell build
+    const int32_t* src_of;     // slot of each entry of the ranges (null: the entries are the slots)
     dp_dev_status* st;
     long long n;
     int kcap;
-    int ccap;
+    int morton;
     int nc[DP_MAX_DIM];
-    double inv_w[DP_MAX_DIM];
     double box[DP_MAX_DIM];
     float unit[DP_MAX_DIM];
     double cutoff;
@@ -321,7 +514,7 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_cells(NlArgs a) {
     uint32_t ui[D];
     dp_shadow_unpack<D>(shi, ui);
     int ci[D];
-    cell_coords<D>(xi, a.nc, a.inv_w, a.box, ci);
+    shadow_cell<D>(ui, a.nc, ci);
     int count = 0;
     int stencil = 1;
 #pragma unroll
@@ -337,11 +530,10 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_cells(NlArgs a) {
             if (c >= a.nc[k]) c -= a.nc[k];
             cj[k] = c;
         }
-        const long long l = cell_linear<D>(cj, a.nc);
-        const int m = min(a.cell_cnt[l], a.ccap);
-        const int32_t* mem = a.cell_mem + l * a.ccap;
-        for (int t = 0; t < m; ++t) {
-            const int j = mem[t];
+        const int key = cell_key<D>(cj, a.nc, a.morton);
+        const int lo = __ldg(a.bin_start + key), hi = __ldg(a.bin_start + key + 1);
+        for (int t = lo; t < hi; ++t) {
+            const int j = a.src_of ? __ldg(a.src_of + t) : t;
             if (a.half ? j <= i : j == i) continue;
             // float32 pre-test on the fixed-point displacement (nearest image,
             // never longer than the single-shift one); float64 only near the cutoff
@@ -476,17 +668,20 @@ __global__ void k_advance_step(dp_dev_status* st, long long steps, int clear_far
     if (clear_far) st->far = 0;
 }
 
-// Rows of the column-major list -> row-major (N, kout), each row sorted
-// ascending and -1 padded (dompap's neighbor_list layout).
+// Rows of the column-major list (in slots) -> row-major (N, kout) by particle
+// id, entries as particle ids, each row sorted ascending and -1 padded
+// (dompap's neighbor_list layout).
 __global__ void k_nl_export(const int32_t* __restrict__ nl, const int32_t* __restrict__ cnt, int32_t* out,
-                            long long n, int kout) {
+                            const int32_t* __restrict__ order, const int32_t* __restrict__ slot_of, long long n,
+                            int kout) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int c = cnt[i];
+    const long long r = slot_of[i];
+    const int c = cnt[r];
     int32_t* row = out + i * kout;
     int m = 0;  // entries kept so far (<= kout), the kout smallest in ascending order
     for (int k = 0; k < c; ++k) {
-        const int32_t v = nl[(long long)k * n + i];
+        const int32_t v = order[nl[(long long)k * n + r]];
         int u;
         if (m < kout) {
             u = m - 1;
@@ -1023,11 +1218,25 @@ struct dp_sim {
     double cutoff = 0.0;
     int nc[DP_MAX_DIM] = {0, 0, 0, 0};
     long long ncell = 0;
-    int ccap = 0;
     int32_t *nl = nullptr, *cnt = nullptr;
     long long nl_alloc = 0;
-    int32_t *cell_cnt = nullptr, *cell_mem = nullptr;
-    long long cell_cnt_alloc = 0, cell_mem_alloc = 0;
+    // cell binning (counting sort): cell keys, Morton or row-major
+    bool morton = false;
+    long long nbins = 0, bins_alloc = 0;
+    int32_t *bin_cnt = nullptr, *bin_start = nullptr, *bin_part = nullptr;
+    int32_t *bin_key = nullptr, *bin_rank = nullptr, *src_of = nullptr;
+    // slots: after each cell-list rebuild the per-particle state is stored in
+    // cell order; order[slot] = particle id, slot_of[id] = slot
+    bool reorder = true;  // DOMPAP_REORDER=0: the state keeps its order, the build reads through src_of
+    int32_t *order = nullptr, *slot_of = nullptr;
+    // scratch of the permutation (vel, beta, img, order, types, mass classes, masses)
+    double *sc_vel = nullptr, *sc_beta = nullptr, *sc_mass = nullptr;
+    int32_t *sc_img = nullptr, *sc_order = nullptr, *sc_types = nullptr;
+    uint8_t* sc_mclass = nullptr;
+    // backup of the permutation-dependent arrays for an overflow replay
+    int32_t *bk_order = nullptr, *bk_types = nullptr;
+    uint8_t* bk_mclass = nullptr;
+    double* bk_mass = nullptr;
     bool nl_config_dirty = true;
     bool nl_built = false;
 
@@ -1164,36 +1373,53 @@ static int configure_nl(dp_sim* s) {
     s->cutoff = reach + s->skin;  // dompap/Simulation.py:353-356
     bool cells = s->method == DP_NL_CELL && std::isfinite(s->cutoff) && s->cutoff > 0;
     long long ncell = 1;
+    int pmax = 1;  // power of two covering the largest cell count
     for (int k = 0; k < s->dim && cells; ++k) {
-        // a relative margin keeps every cell strictly wider than the cutoff
-        const double w = s->cutoff * (1.0 + 1e-10);
+        // cells strictly wider than the cutoff plus the shadow's rounding
+        // (a few L / 2^32): a pair closer than the cutoff is never more than
+        // one cell apart when the cells come from the shadows
+        const double w = s->cutoff * (1.0 + 1e-10) + 8.0 * s->box[k] / 4294967296.0;
         const double ncd = std::floor(s->box[k] / w);
-        if (!(ncd >= 3.0) || ncd > 1e6) {
+        if (!(ncd >= 3.0) || ncd > 65536.0) {
             cells = false;
             break;
         }
         s->nc[k] = (int)ncd;
         ncell *= s->nc[k];
-        if (ncell > (1LL << 31)) cells = false;
+        while (pmax < s->nc[k]) pmax <<= 1;
+        if (ncell > (1LL << 30)) cells = false;
     }
     s->use_cells = cells;
     if (!cells) {
         for (int k = 0; k < DP_MAX_DIM; ++k) s->nc[k] = 0;
         s->ncell = 0;
+        s->nbins = 0;
     } else {
         for (int k = s->dim; k < DP_MAX_DIM; ++k) s->nc[k] = 1;
         s->ncell = ncell;
-        const double avg = (double)s->n / (double)ncell;
-        int cap = (int)std::ceil(avg * 2.0 + 8.0);
-        cap = (cap + 3) & ~3;
-        s->ccap = std::max(s->ccap, cap);
-        if (s->ncell > s->cell_cnt_alloc) {
-            RET(dalloc_t(&s->cell_cnt, (size_t)s->ncell));
-            s->cell_cnt_alloc = s->ncell;
+        // Morton keys on the padded grid while it stays within 2^26 keys and
+        // the bit interleaving's width (16 bits per axis in 2-D, 10 in 3-D, 8 in 4-D)
+        long long padded = 1;
+        for (int k = 0; k < s->dim; ++k) padded *= pmax;
+        const int bits_per_axis = s->dim == 2 ? 16 : (s->dim == 3 ? 10 : 8);
+        s->morton = padded <= (1LL << 26) && pmax <= (1 << bits_per_axis);
+        s->nbins = s->morton ? padded : ncell;
+        if (s->nbins > s->bins_alloc) {
+            RET(dalloc_t(&s->bin_cnt, (size_t)s->nbins));
+            RET(dalloc_t(&s->bin_start, (size_t)s->nbins + 1));
+            RET(dalloc_t(&s->bin_part, (size_t)((s->nbins + kScanTile - 1) / kScanTile)));
+            s->bins_alloc = s->nbins;
         }
-        if (s->ncell * s->ccap > s->cell_mem_alloc) {
-            RET(dalloc_t(&s->cell_mem, (size_t)(s->ncell * s->ccap)));
-            s->cell_mem_alloc = s->ncell * s->ccap;
+        if (!s->bin_key) {
+            const size_t n = (size_t)s->n, nd = n * s->dim;
+            RET(dalloc_t(&s->bin_key, n));
+            RET(dalloc_t(&s->bin_rank, n));
+            RET(dalloc_t(&s->src_of, n));
+            RET(dalloc_t(&s->sc_vel, nd));
+            RET(dalloc_t(&s->sc_beta, nd));
+            RET(dalloc_t(&s->sc_img, nd));
+            RET(dalloc_t(&s->sc_order, n));
+            RET(dalloc_t(&s->bk_order, n));
         }
     }
     const long long need = (long long)s->kcap * s->n;
@@ -1207,19 +1433,50 @@ static int configure_nl(dp_sim* s) {
     return DP_OK;
 }
 
-static void fill_cell_args(const dp_sim* s, CellArgs& a) {
-    a.pos = s->pos;
-    a.cell_cnt = s->cell_cnt;
-    a.cell_mem = s->cell_mem;
-    a.st = s->dstat;
-    a.n = s->n;
-    a.ncell = s->ncell;
-    a.ccap = s->ccap;
-    for (int k = 0; k < DP_MAX_DIM; ++k) {
-        a.nc[k] = s->nc[k];
-        a.inv_w[k] = (k < s->dim && s->nc[k] > 0) ? (double)s->nc[k] / s->box[k] : 0.0;
-        a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
+// Scratch and backup arrays of the optional per-particle arrays (types, mass
+// classes, masses), allocated once those exist.
+static int ensure_perm_extras(dp_sim* s) {
+    const size_t n = (size_t)s->n;
+    if (s->types && !s->sc_types) {
+        RET(dalloc_t(&s->sc_types, n));
+        RET(dalloc_t(&s->bk_types, n));
     }
+    if (s->mclass && !s->sc_mclass) {
+        RET(dalloc_t(&s->sc_mclass, n));
+        RET(dalloc_t(&s->bk_mclass, n));
+    }
+    if (s->mass && !s->sc_mass) {
+        RET(dalloc_t(&s->sc_mass, n));
+        RET(dalloc_t(&s->bk_mass, n));
+    }
+    return DP_OK;
+}
+
+// The state arrays that move with their particle, with their scratch: the
+// positions use the second position set (free during a rebuild: a fused step
+// writes it after the rebuild, the separate integrator does not use it).
+static void fill_perm_args(const dp_sim* s, PermArgs& p) {
+    memset(&p, 0, sizeof(p));
+    const int sh = s->dim == 2 ? 8 : 16;
+    const int p64 = s->dim == 2 ? 16 : 32;
+    auto add = [&](void* data, void* scratch, int esize, int comps) {
+        if (data && scratch) p.arr[p.count++] = PermArray{data, scratch, esize, comps};
+    };
+    add(s->pos, s->pos_alt, 8, s->dim);
+    add(s->shadow, s->shadow_alt, sh, 1);
+    add(s->pos64, s->pos64_alt, p64, 1);
+    add(s->vel, s->sc_vel, 8, s->dim);
+    add(s->beta, s->sc_beta, 8, s->dim);
+    add(s->img, s->sc_img, 4, s->dim);
+    add(s->order, s->sc_order, 4, 1);
+    add(s->types, s->sc_types, 4, 1);
+    add(s->mclass, s->sc_mclass, 1, 1);
+    add(s->mass, s->sc_mass, 8, 1);
+    p.src_of = s->src_of;
+    p.order = s->order;
+    p.slot_of = s->slot_of;
+    p.st = s->dstat;
+    p.n = s->n;
 }
 
 // The gated rebuild sequence (no effect unless need_rebuild is set).
@@ -1236,38 +1493,61 @@ static int launch_rebuild(dp_sim* s, long long* launches) {
     na.shadow_ref = s->shadow_ref;
     na.nl = s->nl;
     na.cnt = s->cnt;
-    na.cell_cnt = s->cell_cnt;
-    na.cell_mem = s->cell_mem;
     na.st = s->dstat;
     na.n = s->n;
     na.kcap = s->kcap;
-    na.ccap = s->ccap;
     na.cutoff = s->cutoff;
     bracket(s, s->cutoff, &na.lo2, &na.hi2);
     fill_scale(s, nullptr, na.unit);
     for (int k = 0; k < DP_MAX_DIM; ++k) na.box[k] = (k < s->dim) ? s->box[k] : 1.0;
     long long nl_launches = 0;
     if (s->use_cells) {
-        CellArgs ca{};
-        fill_cell_args(s, ca);
-        for (int k = 0; k < DP_MAX_DIM; ++k) {
-            na.nc[k] = ca.nc[k];
-            na.inv_w[k] = ca.inv_w[k];
-        }
-        const unsigned gc = (unsigned)std::min<long long>(grid_for(s->ncell, kBlock), 4096);
-        k_cell_clear<<<gc, kBlock, 0, s->stream>>>(ca);
+        // counting sort of the slots by cell key
+        BinArgs ba{};
+        ba.shadow = s->shadow;
+        ba.order = s->order;
+        ba.key = s->bin_key;
+        ba.rank = s->bin_rank;
+        ba.bin_cnt = s->bin_cnt;
+        ba.bin_start = s->bin_start;
+        ba.bin_part = s->bin_part;
+        ba.src_of = s->src_of;
+        ba.st = s->dstat;
+        ba.n = s->n;
+        ba.nbins = s->nbins;
+        ba.morton = s->morton ? 1 : 0;
+        for (int k = 0; k < DP_MAX_DIM; ++k) ba.nc[k] = s->nc[k];
+        const int parts = (int)((s->nbins + kScanTile - 1) / kScanTile);
+        k_bin_clear<<<(unsigned)std::min<long long>(grid_for(s->nbins, kBlock), 8192), kBlock, 0, s->stream>>>(ba);
         switch (s->dim) {
-            case 2: k_cell_fill<2><<<gp, kBlock, 0, s->stream>>>(ca); break;
-            case 3: k_cell_fill<3><<<gp, kBlock, 0, s->stream>>>(ca); break;
-            default: k_cell_fill<4><<<gp, kBlock, 0, s->stream>>>(ca); break;
+            case 2: k_bin_count<2><<<gp, kBlock, 0, s->stream>>>(ba); break;
+            case 3: k_bin_count<3><<<gp, kBlock, 0, s->stream>>>(ba); break;
+            default: k_bin_count<4><<<gp, kBlock, 0, s->stream>>>(ba); break;
         }
-        k_cell_sort<<<grid_for(s->ncell, kBlock), kBlock, 0, s->stream>>>(ca);
+        k_scan_reduce<<<parts, kScanThreads, 0, s->stream>>>(ba);
+        k_scan_top<<<1, kScanThreads, 0, s->stream>>>(ba, parts);
+        k_scan_down<<<parts, kScanThreads, 0, s->stream>>>(ba);
+        k_bin_scatter<<<gp, kBlock, 0, s->stream>>>(ba);
+        k_bin_sort<<<grid_for(s->nbins, kBlock), kBlock, 0, s->stream>>>(ba);
+        nl_launches = 7;
+        if (s->reorder) {
+            // the state into cell order: slot t <- slot src_of[t]
+            PermArgs pa;
+            fill_perm_args(s, pa);
+            k_permute<<<gp, kBlock, 0, s->stream>>>(pa);
+            k_permute_back<<<gp, kBlock, 0, s->stream>>>(pa);
+            nl_launches += 2;
+        }
+        na.bin_start = s->bin_start;
+        na.src_of = s->reorder ? nullptr : s->src_of;
+        na.morton = ba.morton;
+        for (int k = 0; k < DP_MAX_DIM; ++k) na.nc[k] = s->nc[k];
         switch (s->dim) {
             case 2: k_nl_build_cells<2><<<gp, kBlock, 0, s->stream>>>(na); break;
             case 3: k_nl_build_cells<3><<<gp, kBlock, 0, s->stream>>>(na); break;
             default: k_nl_build_cells<4><<<gp, kBlock, 0, s->stream>>>(na); break;
         }
-        nl_launches = 4;
+        nl_launches += 1;
     } else {
         switch (s->dim) {
             case 2: k_nl_build_allpairs<2><<<gp, kBlock, 0, s->stream>>>(na); break;
@@ -1294,6 +1574,7 @@ static void fill_pair_args(const dp_sim* s, dp_pair_args& a, double* out) {
     a.isig_tab = s->isig_tab;
     a.ff_tab = s->ff_tab;
     a.pos64 = s->pos64;
+    a.order = s->order;
     a.out = out;
     a.partial = s->partial;
     a.status = s->dstat;
@@ -1404,6 +1685,7 @@ static void fill_int_args(const dp_sim* s, dp_int_args& a, long long step_offset
     a.mcoef = s->mcoef;
     a.mcoef_f = s->mcoef_f;
     a.mass = s->mass;
+    a.order = s->order;
     a.st = s->dstat;
     a.n = s->n;
     for (int k = 0; k < DP_MAX_DIM; ++k) a.box[k] = (k < s->dim) ? s->box[k] : 1.0;
@@ -1524,15 +1806,6 @@ static int require_ready(dp_sim* s) {
 // Grow capacities after an overflow reported in hstat; returns 1 if grown.
 static int grow_after_overflow(dp_sim* s, bool* grown) {
     *grown = false;
-    if (s->hstat->cell_overflow > 0 && s->use_cells) {
-        s->ccap = ((int)(s->hstat->cell_overflow * 1.5) + 8 + 3) & ~3;
-        if (s->ncell * s->ccap > s->cell_mem_alloc) {
-            RET(dalloc_t(&s->cell_mem, (size_t)(s->ncell * s->ccap)));
-            s->cell_mem_alloc = s->ncell * s->ccap;
-        }
-        s->hstat->cell_overflow = 0;
-        *grown = true;
-    }
     if (s->hstat->max_neighbors > s->kcap) {
         const int want = ((int)(s->hstat->max_neighbors * 1.25) + 32 + 31) & ~31;
         s->kcap = want;
@@ -1553,6 +1826,7 @@ static int grow_after_overflow(dp_sim* s, bool* grown) {
 // Rebuild now if needed (check) or unconditionally; handles overflow growth.
 static int update_nl(dp_sim* s, bool check, int* rebuilt) {
     RET(configure_nl(s));
+    if (s->use_cells) RET(ensure_perm_extras(s));
     RET(read_status(s));
     const long long before = s->hstat->rebuilds;
     if (!s->nl_built || !check || s->nl_half != list_half(s)) {
@@ -1761,23 +2035,36 @@ static int get_graph(dp_sim* s, long long steps, int kind, GraphEntry** out) {
     return DP_OK;
 }
 
+// The state a chunk of steps starts from, for its replay after a list
+// overflow. A rebuild inside the chunk may reorder the slots, so the slot
+// order and the per-particle parameters it moves are saved with the state.
 static int backup_state(dp_sim* s) {
-    const size_t bd = (size_t)s->n * s->dim * sizeof(double);
-    const size_t bi = (size_t)s->n * s->dim * sizeof(int32_t);
+    const size_t n = (size_t)s->n, bd = n * s->dim * sizeof(double), bi = n * s->dim * sizeof(int32_t);
     CK(cudaMemcpyAsync(s->bk_pos, s->pos, bd, cudaMemcpyDeviceToDevice, s->stream));
     CK(cudaMemcpyAsync(s->bk_vel, s->vel, bd, cudaMemcpyDeviceToDevice, s->stream));
     CK(cudaMemcpyAsync(s->bk_beta, s->beta, bd, cudaMemcpyDeviceToDevice, s->stream));
     CK(cudaMemcpyAsync(s->bk_img, s->img, bi, cudaMemcpyDeviceToDevice, s->stream));
+    if (s->bk_order) CK(cudaMemcpyAsync(s->bk_order, s->order, n * 4, cudaMemcpyDeviceToDevice, s->stream));
+    if (s->bk_types && s->types) CK(cudaMemcpyAsync(s->bk_types, s->types, n * 4, cudaMemcpyDeviceToDevice, s->stream));
+    if (s->bk_mclass && s->mclass) CK(cudaMemcpyAsync(s->bk_mclass, s->mclass, n, cudaMemcpyDeviceToDevice, s->stream));
+    if (s->bk_mass && s->mass) CK(cudaMemcpyAsync(s->bk_mass, s->mass, n * 8, cudaMemcpyDeviceToDevice, s->stream));
     return DP_OK;
 }
 
 static int restore_state(dp_sim* s) {
-    const size_t bd = (size_t)s->n * s->dim * sizeof(double);
-    const size_t bi = (size_t)s->n * s->dim * sizeof(int32_t);
+    const size_t n = (size_t)s->n, bd = n * s->dim * sizeof(double), bi = n * s->dim * sizeof(int32_t);
     CK(cudaMemcpyAsync(s->pos, s->bk_pos, bd, cudaMemcpyDeviceToDevice, s->stream));
     CK(cudaMemcpyAsync(s->vel, s->bk_vel, bd, cudaMemcpyDeviceToDevice, s->stream));
     CK(cudaMemcpyAsync(s->beta, s->bk_beta, bd, cudaMemcpyDeviceToDevice, s->stream));
     CK(cudaMemcpyAsync(s->img, s->bk_img, bi, cudaMemcpyDeviceToDevice, s->stream));
+    if (s->bk_order) {
+        CK(cudaMemcpyAsync(s->order, s->bk_order, n * 4, cudaMemcpyDeviceToDevice, s->stream));
+        k_invert_order<<<grid_for(s->n, kBlock), kBlock, 0, s->stream>>>(s->order, s->slot_of, s->n);
+        CK(cudaGetLastError());
+    }
+    if (s->bk_types && s->types) CK(cudaMemcpyAsync(s->types, s->bk_types, n * 4, cudaMemcpyDeviceToDevice, s->stream));
+    if (s->bk_mclass && s->mclass) CK(cudaMemcpyAsync(s->mclass, s->bk_mclass, n, cudaMemcpyDeviceToDevice, s->stream));
+    if (s->bk_mass && s->mass) CK(cudaMemcpyAsync(s->mass, s->bk_mass, n * 8, cudaMemcpyDeviceToDevice, s->stream));
     return launch_shadow(s);
 }
 
@@ -1892,6 +2179,7 @@ int dp_create(int dim, int64_t n, int precision, dp_sim** out) {
     if (const char* env = std::getenv("DOMPAP_FUSED_STEP")) s->fused_step = std::atoi(env) != 0;
     if (const char* env = std::getenv("DOMPAP_WARP_STEP")) s->warp_step_max = std::atoll(env);
     if (const char* env = std::getenv("DOMPAP_QUAD_STEP")) s->quad_step_max = std::atoll(env);
+    if (const char* env = std::getenv("DOMPAP_REORDER")) s->reorder = std::atoi(env) != 0;
     if (const char* env = std::getenv("DOMPAP_MLP_TENSOR"))
         s->mlp_tensor = std::strcmp(env, "tcgen05") == 0 ? 1 : (std::strcmp(env, "mma") == 0 ? 2 : 0);
     int rc = DP_OK;
@@ -1909,8 +2197,10 @@ int dp_create(int dim, int64_t n, int precision, dp_sim** out) {
     if ((rc = dalloc_t(&s->pos, nd)) || (rc = dalloc_t(&s->vel, nd)) || (rc = dalloc_t(&s->beta, nd)) ||
         (rc = dalloc_t(&s->force, nd)) || (rc = dalloc_t(&s->pos_ref, nd)) || (rc = dalloc_t(&s->img, nd)) ||
         (rc = dalloc_t(&s->bk_pos, nd)) || (rc = dalloc_t(&s->bk_vel, nd)) || (rc = dalloc_t(&s->bk_beta, nd)) ||
-        (rc = dalloc_t(&s->bk_img, nd)) || (rc = dalloc_t(&s->cnt, (size_t)n)))
+        (rc = dalloc_t(&s->bk_img, nd)) || (rc = dalloc_t(&s->cnt, (size_t)n)) ||
+        (rc = dalloc_t(&s->order, (size_t)n)) || (rc = dalloc_t(&s->slot_of, (size_t)n)))
         return cleanup();
+    k_iota<<<grid_for(n, kBlock), kBlock, 0, s->stream>>>(s->order, s->slot_of, n);  // slot = particle id
     s->shadow_bytes = (size_t)n * (dim == 2 ? 8 : 16);
     if ((rc = dalloc(&s->shadow, s->shadow_bytes)) || (rc = dalloc(&s->shadow_ref, s->shadow_bytes)) ||
         (rc = dalloc(&s->pos64, (size_t)n * (dim == 2 ? 16 : 32))) || (rc = dalloc_t(&s->pos_alt, nd)) ||
@@ -1952,7 +2242,10 @@ int dp_destroy(dp_sim* s) {
                     s->pos_alt, s->shadow_alt, s->pos64_alt, s->mlp_fx,
                     s->ff_tab, s->bk_pos,
                     s->bk_vel, s->bk_beta, s->bk_img, s->mclass, s->mcoef, s->mcoef_f, s->class_mass_dev, s->mass, s->types,
-                    s->sig_tab, s->eps_tab, s->isig_tab, s->nl, s->cnt, s->cell_cnt, s->cell_mem, s->dstat,
+                    s->sig_tab, s->eps_tab, s->isig_tab, s->nl, s->cnt, s->bin_cnt, s->bin_start, s->bin_part,
+                    s->bin_key, s->bin_rank, s->src_of, s->order, s->slot_of, s->sc_vel, s->sc_beta, s->sc_mass,
+                    s->sc_img, s->sc_order, s->sc_types, s->sc_mclass, s->bk_order, s->bk_types, s->bk_mclass,
+                    s->bk_mass, s->dstat,
                     s->partial, s->dsum};
     for (void* b : bufs)
         if (b) cudaFree(b);
@@ -1995,21 +2288,25 @@ static const void* mapped_view(const void* host) {
     return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
 }
 
-// host AoS (n, dim) -> device SoA; the caller synchronises (the host array
-// must not change before that).
-static int upload_aos_f64_async(dp_sim* s, const double* host, double* dev_soa) {
+// host (n, comps) in particle-id order -> device SoA in slot order; the
+// caller synchronises (the host array must not change before that).
+static int upload_f64_async(dp_sim* s, const double* host, double* dev_soa, int comps) {
     if (!host) return fail(DP_ERR_ARG, "null array");
-    const unsigned g = grid_for(s->n * s->dim, kBlock);
+    const unsigned g = grid_for(s->n * comps, kBlock);
     if (const double* view = (const double*)mapped_view(host)) {
-        k_aos_to_soa_f64<<<g, kBlock, 0, s->stream>>>(view, dev_soa, s->n, s->dim);
+        k_host_to_slots<double><<<g, kBlock, 0, s->stream>>>(view, dev_soa, s->slot_of, s->n, comps);
     } else {
         // stage through the backup buffer to transpose on the device
-        CK(cudaMemcpyAsync(s->bk_pos, host, (size_t)s->n * s->dim * sizeof(double), cudaMemcpyHostToDevice,
+        CK(cudaMemcpyAsync(s->bk_pos, host, (size_t)s->n * comps * sizeof(double), cudaMemcpyHostToDevice,
                            s->stream));
-        k_aos_to_soa_f64<<<g, kBlock, 0, s->stream>>>(s->bk_pos, dev_soa, s->n, s->dim);
+        k_host_to_slots<double><<<g, kBlock, 0, s->stream>>>(s->bk_pos, dev_soa, s->slot_of, s->n, comps);
     }
     CK(cudaGetLastError());
     return DP_OK;
+}
+
+static int upload_aos_f64_async(dp_sim* s, const double* host, double* dev_soa) {
+    return upload_f64_async(s, host, dev_soa, s->dim);
 }
 
 static int upload_aos_f64(dp_sim* s, const double* host, double* dev_soa) {
@@ -2018,24 +2315,41 @@ static int upload_aos_f64(dp_sim* s, const double* host, double* dev_soa) {
     return DP_OK;
 }
 
-// device SoA -> host AoS (n, dim); the caller synchronises before reading it.
-static int download_aos_f64_async(dp_sim* s, const double* dev_soa, double* host) {
+// device SoA in slot order -> host (n, comps) in particle-id order; the
+// caller synchronises before reading it.
+static int download_f64_async(dp_sim* s, const double* dev_soa, double* host, int comps) {
     if (!host) return fail(DP_ERR_ARG, "null array");
-    const unsigned g = grid_for(s->n * s->dim, kBlock);
+    const unsigned g = grid_for(s->n * comps, kBlock);
     if (double* view = (double*)mapped_view(host)) {
-        k_soa_to_aos_f64<<<g, kBlock, 0, s->stream>>>(dev_soa, view, s->n, s->dim);
+        k_slots_to_host<double><<<g, kBlock, 0, s->stream>>>(dev_soa, view, s->slot_of, s->n, comps);
         CK(cudaGetLastError());
     } else {
-        k_soa_to_aos_f64<<<g, kBlock, 0, s->stream>>>(dev_soa, s->bk_vel, s->n, s->dim);
+        k_slots_to_host<double><<<g, kBlock, 0, s->stream>>>(dev_soa, s->bk_vel, s->slot_of, s->n, comps);
         CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(host, s->bk_vel, (size_t)s->n * s->dim * sizeof(double), cudaMemcpyDeviceToHost,
+        CK(cudaMemcpyAsync(host, s->bk_vel, (size_t)s->n * comps * sizeof(double), cudaMemcpyDeviceToHost,
                            s->stream));
     }
     return DP_OK;
 }
 
+static int download_aos_f64_async(dp_sim* s, const double* dev_soa, double* host) {
+    return download_f64_async(s, dev_soa, host, s->dim);
+}
+
 static int download_aos_f64(dp_sim* s, const double* dev_soa, double* host) {
     RET(download_aos_f64_async(s, dev_soa, host));
+    CK(cudaStreamSynchronize(s->stream));
+    return DP_OK;
+}
+
+// host int32 (n, comps) in id order -> device SoA in slot order, staged
+// through bk_img (n * dim int32, comps <= dim).
+static int upload_i32(dp_sim* s, const int32_t* host, int32_t* dev_soa, int comps) {
+    const size_t bytes = (size_t)s->n * comps * sizeof(int32_t);
+    CK(cudaMemcpyAsync(s->bk_img, host, bytes, cudaMemcpyHostToDevice, s->stream));
+    k_host_to_slots<int32_t><<<grid_for(s->n * comps, kBlock), kBlock, 0, s->stream>>>(s->bk_img, dev_soa, s->slot_of,
+                                                                                         s->n, comps);
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s->stream));
     return DP_OK;
 }
@@ -2073,17 +2387,13 @@ int dp_get_betas(dp_sim* s, double* b) {
 }
 int dp_set_images(dp_sim* s, const int32_t* im) {
     if (!s || !im) return fail(DP_ERR_ARG, "null argument");
-    const size_t bytes = (size_t)s->n * s->dim * sizeof(int32_t);
-    CK(cudaMemcpyAsync(s->bk_img, im, bytes, cudaMemcpyHostToDevice, s->stream));
-    k_aos_to_soa_i32<<<grid_for(s->n * s->dim, kBlock), kBlock, 0, s->stream>>>(s->bk_img, s->img, s->n, s->dim);
-    CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(s->stream));
-    return DP_OK;
+    return upload_i32(s, im, s->img, s->dim);
 }
 int dp_get_images(dp_sim* s, int32_t* im) {
     if (!s || !im) return fail(DP_ERR_ARG, "null argument");
     const size_t bytes = (size_t)s->n * s->dim * sizeof(int32_t);
-    k_soa_to_aos_i32<<<grid_for(s->n * s->dim, kBlock), kBlock, 0, s->stream>>>(s->img, s->bk_img, s->n, s->dim);
+    k_slots_to_host<int32_t><<<grid_for(s->n * s->dim, kBlock), kBlock, 0, s->stream>>>(s->img, s->bk_img,
+                                                                                         s->slot_of, s->n, s->dim);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(im, s->bk_img, bytes, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -2107,13 +2417,19 @@ int dp_set_masses(dp_sim* s, const double* m) {
         }
         std::vector<uint8_t> cls((size_t)s->n);
         for (long long i = 0; i < s->n; ++i) cls[i] = (uint8_t)classes[m[i]];
-        RET(dalloc_t(&s->mclass, (size_t)s->n));
-        CK(cudaMemcpy(s->mclass, cls.data(), (size_t)s->n, cudaMemcpyHostToDevice));
+        if (!s->mclass) RET(dalloc_t(&s->mclass, (size_t)s->n));
+        // by particle id into the slot order (staged through bk_img)
+        CK(cudaMemcpyAsync(s->bk_img, cls.data(), (size_t)s->n, cudaMemcpyHostToDevice, s->stream));
+        k_host_to_slots<uint8_t><<<grid_for(s->n, kBlock), kBlock, 0, s->stream>>>(
+            (const uint8_t*)s->bk_img, s->mclass, s->slot_of, s->n, 1);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(s->stream));
     } else {
         s->mass_mode = 2;
         s->class_mass.assign(1, m[0]);
-        RET(dalloc_t(&s->mass, (size_t)s->n));
-        CK(cudaMemcpy(s->mass, m, (size_t)s->n * sizeof(double), cudaMemcpyHostToDevice));
+        if (!s->mass) RET(dalloc_t(&s->mass, (size_t)s->n));
+        RET(upload_f64_async(s, m, s->mass, 1));
+        CK(cudaStreamSynchronize(s->stream));
     }
     if (s->mass_mode == 2) {
         // the reduction kernels read per-particle masses
@@ -2136,7 +2452,7 @@ int dp_set_types(dp_sim* s, const int32_t* t) {
     s->min_type = lo;
     s->max_type = hi;
     if (!s->types) RET(dalloc_t(&s->types, (size_t)s->n));
-    CK(cudaMemcpy(s->types, t, (size_t)s->n * sizeof(int32_t), cudaMemcpyHostToDevice));
+    RET(upload_i32(s, t, s->types, 1));
     s->have_types = true;
     s->version++;
     return DP_OK;
@@ -2341,7 +2657,7 @@ int dp_get_neighbor_list(dp_sim* s, int32_t* out, int kmax, int32_t* max_count) 
     int32_t* dout = nullptr;
     if (e == cudaSuccess && dalloc_t(&dout, (size_t)s->n * kmax) != DP_OK) e = cudaErrorMemoryAllocation;
     if (e == cudaSuccess) {
-        k_nl_export<<<g, kBlock, 0, s->stream>>>(rows, counts, dout, s->n, kmax);
+        k_nl_export<<<g, kBlock, 0, s->stream>>>(rows, counts, dout, s->order, s->slot_of, s->n, kmax);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)
@@ -2454,7 +2770,7 @@ int dp_laplacian(dp_sim* s, double* lap) {
     if (!lap) return fail(DP_ERR_ARG, "null output");
     RET(update_nl(s, true, nullptr));
     RET(launch_pair(s, s->lib.laplacian, s->bk_beta, nullptr));
-    CK(cudaMemcpyAsync(lap, s->bk_beta, (size_t)s->n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    RET(download_f64_async(s, s->bk_beta, lap, 1));
     CK(cudaStreamSynchronize(s->stream));
     return DP_OK;
 }
@@ -2534,7 +2850,7 @@ int dp_get_stats(dp_sim* s, dp_stats* st) {
     st->max_neighbors = s->hstat->max_neighbors;
     st->neighbor_capacity = s->kcap;
     for (int k = 0; k < 4; ++k) st->cells[k] = s->use_cells ? s->nc[k] : 0;
-    st->cell_capacity = s->ccap;
+    st->cell_capacity = 0;  // cells are contiguous slot ranges: no capacity
     st->method_used = s->use_cells ? DP_NL_CELL : DP_NL_ALLPAIRS;
     st->nl_cutoff = s->cutoff;
     st->conditional_graphs = s->conditional_graphs ? 1 : 0;
@@ -3029,9 +3345,9 @@ int dp_batch_set_state(dp_batch* b, const double* positions, const double* veloc
     CK(cudaMemcpy(b->box, b->h_box.data(), b->h_box.size() * 8, cudaMemcpyHostToDevice));
     const unsigned g = grid_for(b->ntot * b->dim, kBlock);
     CK(cudaMemcpyAsync(b->stage, positions, bytes, cudaMemcpyHostToDevice, b->stream));
-    k_aos_to_soa_f64<<<g, kBlock, 0, b->stream>>>(b->stage, b->pos, b->ntot, b->dim);
+    k_host_to_slots<double><<<g, kBlock, 0, b->stream>>>(b->stage, b->pos, nullptr, b->ntot, b->dim);
     CK(cudaMemcpyAsync(b->stage, velocities, bytes, cudaMemcpyHostToDevice, b->stream));
-    k_aos_to_soa_f64<<<g, kBlock, 0, b->stream>>>(b->stage, b->vel, b->ntot, b->dim);
+    k_host_to_slots<double><<<g, kBlock, 0, b->stream>>>(b->stage, b->vel, nullptr, b->ntot, b->dim);
     k_batch_shadow<<<grid_for(b->ntot, kBlock), kBlock, 0, b->stream>>>(b->pos, b->shadow, b->rep_of, b->box, b->dim,
                                                                         b->ntot);
     CK(cudaGetLastError());
@@ -3046,18 +3362,18 @@ int dp_batch_get_state(dp_batch* b, double* positions, double* velocities, int32
     const size_t bytes = (size_t)b->ntot * b->dim * sizeof(double);
     const unsigned g = grid_for(b->ntot * b->dim, kBlock);
     if (positions) {
-        k_soa_to_aos_f64<<<g, kBlock, 0, b->stream>>>(b->pos, b->stage, b->ntot, b->dim);
+        k_slots_to_host<double><<<g, kBlock, 0, b->stream>>>(b->pos, b->stage, nullptr, b->ntot, b->dim);
         CK(cudaMemcpyAsync(positions, b->stage, bytes, cudaMemcpyDeviceToHost, b->stream));
         CK(cudaStreamSynchronize(b->stream));
     }
     if (velocities) {
-        k_soa_to_aos_f64<<<g, kBlock, 0, b->stream>>>(b->vel, b->stage, b->ntot, b->dim);
+        k_slots_to_host<double><<<g, kBlock, 0, b->stream>>>(b->vel, b->stage, nullptr, b->ntot, b->dim);
         CK(cudaMemcpyAsync(velocities, b->stage, bytes, cudaMemcpyDeviceToHost, b->stream));
         CK(cudaStreamSynchronize(b->stream));
     }
     if (images) {
         int32_t* st = (int32_t*)b->stage;
-        k_soa_to_aos_i32<<<g, kBlock, 0, b->stream>>>(b->img, st, b->ntot, b->dim);
+        k_slots_to_host<int32_t><<<g, kBlock, 0, b->stream>>>(b->img, st, nullptr, b->ntot, b->dim);
         CK(cudaMemcpyAsync(images, st, (size_t)b->ntot * b->dim * 4, cudaMemcpyDeviceToHost, b->stream));
         CK(cudaStreamSynchronize(b->stream));
     }

@@ -44,6 +44,7 @@ struct dp_pair_args {
     const double* isig_tab;  // 1 / sigma per type pair (DP_PMODE == 1)
     const float2* ff_tab;    // DP_PMODE == 1: (sigma, 1/sigma, epsilon) as double-float triples
     const void* pos64;       // 64-bit fixed-point positions (X = x 2^64 / L), one vector per particle
+    const int32_t* order;    // particle id held by each slot (slots are in cell order after a rebuild)
     double* out;
     double* partial;
     dp_dev_status* status;

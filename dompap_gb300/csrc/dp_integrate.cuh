@@ -26,6 +26,7 @@ struct dp_int_args {
     const double* mcoef;    // massmode 1: [class][5]: a, b dt/m, b/(2m), sqrt(2 alpha T dt), dt/m
     const float2* mcoef_f;  // massmode 1: [class]: float32 b/(2m), sqrt(2 alpha T dt)
     const double* mass;     // massmode 2: mass per particle
+    const int32_t* order;   // particle id held by each slot: keys its Langevin noise
     dp_dev_status* st;
     long long n;
     double box[DP_MAX_DIM];
@@ -141,7 +142,8 @@ __device__ __forceinline__ bool dp_integrate_one(const dp_int_args& a, long long
     float cf[2];
     dp_load_coef<MASSMODE>(a, i, c, cf);
     float z[4];
-    if (!NVE) dp_normals4(a.seed, (unsigned long long)(a.st->step + a.step_offset), (uint32_t)i, z);
+    // the noise of a particle depends on its id, not on the slot it occupies
+    if (!NVE) dp_normals4(a.seed, (unsigned long long)(a.st->step + a.step_offset), (uint32_t)a.order[i], z);
     // every load is issued before the first store (the arrays are not
     // declared non-aliasing, so a store would otherwise order the loads of
     // the next axis behind it)

@@ -56,9 +56,11 @@ __device__ __forceinline__ void dp_pair_params(const dp_pair_args& a, long long 
     isig = __ldg(a.isig_tab + ti * a.ntypes + tj);
     eps = __ldg(a.eps_tab + ti * a.ntypes + tj);
 #else
-    sig = __ldg(a.sig_tab + i * a.n + j);
+    // the dense (N, N) tables are indexed by particle id
+    const long long pi = __ldg(a.order + i), pj = __ldg(a.order + j);
+    sig = __ldg(a.sig_tab + pi * a.n + pj);
     isig = 1.0 / sig;
-    eps = __ldg(a.eps_tab + i * a.n + j);
+    eps = __ldg(a.eps_tab + pi * a.n + pj);
 #endif
 }
 
