@@ -124,6 +124,8 @@ _SIGNATURES = {
     "dp_time_kernel": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "dp_time_forces": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "dp_kernel_launches": (ctypes.c_int64, [_P]),
+    "dp_set_step_launch": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
+    "dp_get_step_launch": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "dp_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _I32, ctypes.POINTER(_P)]),
     "dp_batch_destroy": (ctypes.c_int, [_P]),
     "dp_batch_set_state": (ctypes.c_int, [_P, _D, _D, _D, _D]),

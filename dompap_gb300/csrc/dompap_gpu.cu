@@ -1154,6 +1154,11 @@ struct dp_sim {
     // (dp_step_quad); DOMPAP_WARP_STEP / DOMPAP_QUAD_STEP set them (0: never)
     long long warp_step_max = 8192;
     long long quad_step_max = 65536;
+    // launch shape set by the autotuner (dp_set_step_launch): lanes per
+    // particle of the fused step (0: the size thresholds above) and resident
+    // CTAs per SM it is compiled for (0: the measured default per mode)
+    int step_lanes = 0;
+    int step_blocks = 0;
     // surrogate pass: 0 = tcgen05 from 65,536 particles (the 128-particle CTAs
     // fill the GPU; on par with mma.sync there), mma.sync below; 1 = tcgen05;
     // 2 = mma.sync (DOMPAP_MLP_TENSOR=tcgen05 | mma)
@@ -1916,11 +1921,13 @@ static int launch_step(dp_sim* s, int kind, long long step_offset, long long* la
     ia.shadow_out = s->shadow_alt;
     ia.pos64_out = s->pos64_alt;
     void* args[] = {&pa, &ia};
-    if (s->n <= s->warp_step_max && s->lib.step_warp) {
+    const int lanes = s->step_lanes ? s->step_lanes
+                                    : (s->n <= s->warp_step_max ? 32 : (s->n <= s->quad_step_max ? 4 : 1));
+    if (lanes == 32 && s->lib.step_warp) {
         // small system: one warp per particle (32 n threads)
         CK(cudaLaunchKernel((const void*)s->lib.step_warp, dim3(grid_for(s->n * 32, kBlock)), dim3(kBlock), args, 0,
                             s->stream));
-    } else if (s->n <= s->quad_step_max && s->lib.step_quad) {
+    } else if (lanes == 4 && s->lib.step_quad) {
         CK(cudaLaunchKernel((const void*)s->lib.step_quad, dim3(grid_for(s->n * 4, kBlock)), dim3(kBlock), args, 0,
                             s->stream));
     } else {
@@ -2529,7 +2536,7 @@ static int step_blocks_for(int dim, int precision, int pmode) {
 static int rebuild_pair_lib(dp_sim* s) {
     const bool sig_one = s->pmode == DP_PAIR_CONST && s->sigma == 1.0;
     const bool eps_one = s->pmode == DP_PAIR_CONST && s->epsilon == 1.0;
-    const int step_blocks = step_blocks_for(s->dim, s->precision, s->pmode);
+    const int step_blocks = s->step_blocks ? s->step_blocks : step_blocks_for(s->dim, s->precision, s->pmode);
     const std::string src =
         pair_program(s->dim, s->precision, s->pmode, sig_one, eps_one, s->pot_src, false, step_blocks);
     PairLib pl;
@@ -2537,6 +2544,29 @@ static int rebuild_pair_lib(dp_sim* s) {
     s->lib = pl;
     s->lib_valid = true;
     s->version++;
+    return DP_OK;
+}
+
+int dp_set_step_launch(dp_sim* s, int lanes, int blocks_per_sm) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    if (lanes != 0 && lanes != 1 && lanes != 4 && lanes != 32) return fail(DP_ERR_ARG, "lanes must be 0, 1, 4 or 32");
+    if (blocks_per_sm < 0 || blocks_per_sm > 8) return fail(DP_ERR_ARG, "blocks_per_sm must be in [0, 8]");
+    if (lanes != s->step_lanes) {
+        s->step_lanes = lanes;
+        s->version++;
+    }
+    if (blocks_per_sm != s->step_blocks) {
+        s->step_blocks = blocks_per_sm;
+        if (s->have_pot) RET(rebuild_pair_lib(s));
+    }
+    return DP_OK;
+}
+
+int dp_get_step_launch(dp_sim* s, int* lanes, int* blocks_per_sm) {
+    if (!s || !lanes || !blocks_per_sm) return fail(DP_ERR_ARG, "null argument");
+    *lanes = s->step_lanes ? s->step_lanes
+                           : (s->n <= s->warp_step_max ? 32 : (s->n <= s->quad_step_max ? 4 : 1));
+    *blocks_per_sm = s->step_blocks ? s->step_blocks : step_blocks_for(s->dim, s->precision, s->pmode);
     return DP_OK;
 }
 

@@ -199,6 +199,9 @@ class Simulation:
         _lib.check(lib.dp_create(dim, n, create_prec, _lib.ctypes.byref(h)))
         d["_h"] = h
         d["_h_shape"] = (n, dim)
+        lanes, blocks = d.get("_step_launch", (0, 0))
+        if lanes or blocks:
+            _lib.check(lib.dp_set_step_launch(h, int(lanes), int(blocks)))
         d["_nl_count_base"] += rebuilds
         d["_dev_rebuilds_base"] = 0
         d["_dev_newer"].clear()
@@ -656,6 +659,21 @@ class Simulation:
         _lib.check(self._lib().dp_run(self._h, int(steps), _lib.DP_INT_NVE))
         self._mark_device_newer()
         self.number_of_steps += int(steps)
+
+    def set_step_launch(self, lanes_per_particle: int = 0, blocks_per_sm: int = 0) -> None:
+        """Launch shape of the fused step kernel (extension; set by
+        ``tools.autotune``): lanes per particle 1, 4 or 32 (0: by system size)
+        and resident 256-thread CTAs per SM it is compiled for (0: default)."""
+        self.__dict__["_step_launch"] = (int(lanes_per_particle), int(blocks_per_sm))
+        self._push()
+        _lib.check(self._lib().dp_set_step_launch(self._h, int(lanes_per_particle), int(blocks_per_sm)))
+
+    def get_step_launch(self) -> tuple[int, int]:
+        """(lanes per particle, resident CTAs per SM) of the fused step in use."""
+        self._push()
+        lanes, blocks = _lib.ctypes.c_int(0), _lib.ctypes.c_int(0)
+        _lib.check(self._lib().dp_get_step_launch(self._h, _lib.ctypes.byref(lanes), _lib.ctypes.byref(blocks)))
+        return int(lanes.value), int(blocks.value)
 
     def run_timed(self, steps: int, kind: str = "gjf") -> float:
         """Run and return the device time in ms (CUDA events on the system's stream)."""

@@ -5,9 +5,14 @@ Same procedure as dompap's: time the two neighbour-list build methods (best of
 of ``step_skin`` while the time of ``steps`` steps keeps falling (up to half
 the smallest box side), and keep the fastest setting. Timings of runs are
 device times (CUDA events on the system's stream); builds are timed on the
-host around the synchronous rebuild call. All of dompap's force methods map to
-the same GPU neighbour-list kernel, so ``test_double_loop`` only affects the
-report.
+host around the synchronous rebuild call.
+
+dompap then times its force methods on the system (autotune.py:112-162). On
+the GPU every force method is the same neighbour-list step kernel, so the
+candidates timed here are that kernel's launch shapes instead: one thread,
+four lanes or a warp per particle (the particle's list split over the lanes),
+then the resident CTAs per SM it is compiled for (4 or 6); the fastest is set
+on the system (``Simulation.set_step_launch``).
 """
 from __future__ import annotations
 
@@ -60,6 +65,35 @@ def autotune(sim, steps=100, test_double_loop=True, smallest_skin=0.1, step_skin
     if verbose:
         print(f"Optimal parameters: skin={best}")
     sim.set_neighbor_list(skin=best, method_str=fastest_method)
+
+    # launch shape of the step kernel (the GPU's force-method candidates)
+    sim_copy.set_neighbor_list(skin=best, method_str=fastest_method)
+    n = sim_copy.number_of_particles()
+    lane_candidates = [1] + ([4] if n <= 4_000_000 else []) + ([32] if n <= 262_144 else [])
+    shape_times = {}
+
+    def time_shape(lanes, blocks):
+        sim_copy.set_step_launch(lanes, blocks)
+        sim_copy.run(steps)  # graph capture and warm-up
+        shape_times[(lanes, blocks)] = min(sim_copy.run_timed(steps) for _ in range(2)) / 1000.0
+
+    for lanes in lane_candidates:
+        time_shape(lanes, 0)
+    best_lanes = min(shape_times, key=shape_times.get)[0]
+    default_blocks = sim_copy.get_step_launch()[1]
+    for blocks in (4, 6):
+        if blocks != default_blocks:
+            time_shape(best_lanes, blocks)
+    best_shape = min(shape_times, key=shape_times.get)
+    if verbose:
+        print("Lanes per particle | CTAs per SM | Time per step (ms)")
+        for (lanes, blocks), t in shape_times.items():
+            print(f"{lanes:18d} | {blocks if blocks else default_blocks:11d} | {t / steps * 1000:8.5f}")
+        print(f"Fastest step launch: {best_shape[0]} lanes per particle, "
+              f"{best_shape[1] if best_shape[1] else default_blocks} CTAs per SM")
+    sim.set_step_launch(*best_shape)
+    sim.__dict__["_autotune_results"] = {"neighbor_list_build_s": results, "skins": skins, "skin_times_s": times,
+                                         "step_launch_times_s": shape_times, "step_launch": best_shape}
     if plot:
         try:
             import matplotlib.pyplot as plt

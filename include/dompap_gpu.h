@@ -217,6 +217,17 @@ int dp_time_forces(dp_sim *sim, int reps, float *ms_per_launch);
 int dp_sum_mv2_noalloc(const double *velocities, const double *masses, int64_t n, int dim, double *out,
                        void *stream);
 
+/* Launch shape of the fused step kernel, chosen by the autotuner
+ * (dompap/tools/autotune.py:112-162 times dompap's force methods on the
+ * actual system; here the candidates are launch shapes of the one GPU step):
+ * lanes per particle 1 (one thread per particle), 4 or 32 (the particle's
+ * list split over a lane group), 0 = by system size (32 up to 8,192
+ * particles, 4 up to 65,536, else 1); blocks_per_sm = resident 256-thread
+ * CTAs per SM the step is compiled for (1..8; 0 = the default of the mode;
+ * a change recompiles the pair program). dp_get_step_launch reports the shape
+ * in use. */
+int dp_set_step_launch(dp_sim *sim, int lanes, int blocks_per_sm);
+int dp_get_step_launch(dp_sim *sim, int *lanes, int *blocks_per_sm);
 /* Number of kernels the last dp_run launched (graph nodes included). */
 int64_t dp_kernel_launches(dp_sim *sim);
 
