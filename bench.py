@@ -65,9 +65,10 @@ def expensive_string(r_cut=3.0):
     return f"{EXPENSIVE_RAW} - ({u_rc!r}) - (r - {float(r_cut)!r})*({du_rc!r})"
 
 
-def host_state(name, seed):
+def host_state(name, seed, shuffle=False):
     """Lattice + jitter + Maxwell-Boltzmann velocities, as dompap builds it
-    (set_positions -> set_density -> jitter -> wrap)."""
+    (set_positions -> set_density -> jitter -> wrap). ``shuffle``: the
+    particle ids randomly permuted (input in no spatial order)."""
     from dompap_gb300.positions import generate_positions
 
     dim, unit, cells, rho, pot, rc, skin, T, dt, tau, jitter = WORKLOADS[name]
@@ -83,14 +84,17 @@ def host_state(name, seed):
     img = shift.astype(np.int32)
     pos = pos - shift * box
     vel = rng.normal(0.0, np.sqrt(T), size=pos.shape)
+    if shuffle:
+        p = np.random.default_rng(seed + 1).permutation(pos.shape[0])
+        pos, vel, img = pos[p], vel[p], img[p]
     return pos, vel, img, box
 
 
-def build_sim(name, seed, precision="fp64"):
+def build_sim(name, seed, precision="fp64", shuffle=False):
     from dompap_gb300 import Simulation
 
     dim, unit, cells, rho, pot, rc, skin, T, dt, tau, jitter = WORKLOADS[name]
-    pos, vel, img, box = host_state(name, seed)
+    pos, vel, img, box = host_state(name, seed, shuffle)
     np.random.seed(seed)
     sim = Simulation(precision=precision)
     n = pos.shape[0]
@@ -230,7 +234,7 @@ def e2e_run(sim, steps):
 
 
 # ------------------------------------------------------------------ CPU port
-def cpu_port_run(name, steps, warmup, seed, max_seconds=None):
+def cpu_port_run(name, steps, warmup, seed, max_seconds=None, shuffle=False):
     """Reference algorithm on the host cores: per step skin test (serial),
     neighbour-list rebuild when due (dompap's serial 3-D cell list, or the
     prange double loop for D != 3), prange force loop, serial G-JF and wrap."""
@@ -239,7 +243,7 @@ def cpu_port_run(name, steps, warmup, seed, max_seconds=None):
     dim, unit, cells, rho, pot, rc, skin, T, dt, tau, jitter = WORKLOADS[name]
     lib = cport.load()
     fptr = cport.compile_potential(pot, rc)
-    pos, vel, img, box = host_state(name, seed)
+    pos, vel, img, box = host_state(name, seed, shuffle)
     n = pos.shape[0]
     kmax = 16 if dim == 3 else (8 if dim == 2 else 24)
     if name == "lj500":
@@ -294,10 +298,10 @@ def cpu_port_run(name, steps, warmup, seed, max_seconds=None):
             "threads": lib.dp_port_threads()}
 
 
-def cpu_baseline(name, seed, gpu_steps_per_rebuild):
+def cpu_baseline(name, seed, gpu_steps_per_rebuild, shuffle=False):
     """Bounded sample (about 10-30 s) of the CPU port; the rebuild cost is
     amortised with the steps-per-rebuild the GPU run measured."""
-    r = cpu_port_run(name, steps=1000000, warmup=1, seed=seed, max_seconds=12.0)
+    r = cpu_port_run(name, steps=1000000, warmup=1, seed=seed, max_seconds=12.0, shuffle=shuffle)
     per_step = (r["seconds"] - r["rebuilds"] * r["build_seconds"]) / r["steps"]
     per_step = max(per_step, 1e-12) + r["build_seconds"] / max(gpu_steps_per_rebuild, 1.0)
     return {"value": r["n"] / per_step, "unit": UNIT, "cores": r["threads"], "kind": "port",
@@ -312,14 +316,15 @@ def reference_arm(args):
     if rank != 0:
         return
     name = args.workload
-    r = cpu_port_run(name, steps=args.steps, warmup=args.warmup, seed=args.seed, max_seconds=90.0)
+    r = cpu_port_run(name, steps=args.steps, warmup=args.warmup, seed=args.seed, max_seconds=90.0,
+                     shuffle=args.shuffle_ids)
     value = r["n"] * r["steps"] / r["seconds"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": r["steps"], "warmup": args.warmup, "ms_per_step": 1000 * r["seconds"] / r["steps"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": DATA,
-        "config": config_of(name, int(os.environ.get("WORLD_SIZE", "1"))),
+        "config": config_of(name, int(os.environ.get("WORLD_SIZE", "1")), args.shuffle_ids),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["threads"], "kind": "port",
                          "sample": (f"{r['steps']} full MD steps (rebuilds {r['rebuilds']} included) of the "
                                     f"{r['n']}-particle system; C/OpenMP restatement of dompap's loops "
@@ -478,32 +483,119 @@ def dimension_variant(name, seed, steps, warmup):
     return out
 
 
-def wahnstrom_variant(seed, steps=300, warmup=20):
+def wahnstrom_variant(seed, steps=100000, warmup=20):
     """Binary LJ 50:50 on a simple-cubic (80, 80, 40) lattice = 256,000 at density
     0.75, sigma AA/AB/BB = 1.0/1.1/1.2, masses 2:1, r_cut = 2.5 sigma, T = 0.7,
-    dt = 0.004, damping 0.2, skin 0.5; per-type g(r) after the run."""
+    dt = 0.004, damping 0.2, skin 0.5, the configuration's 100,000 steps timed;
+    per-type g(r) after the run; the CPU port on a bounded sample of the same
+    system (rebuild amortised with the GPU's steps per rebuild)."""
     rng = np.random.default_rng(seed)
     sim = _lattice_sim(((0.0, 0.0, 0.0),), (80, 80, 40), 0.75, "4*(r**-12-r**-6)", 2.5, 0.5, 0.7, 0.004, 0.2,
                        seed, 0.02)
     n = sim.number_of_particles()
     types = np.zeros(n, dtype=np.int32)
     types[rng.permutation(n)[: n // 2]] = 1
+    masses = np.where(types == 0, 2.0, 1.0)
+    sig_t = np.array([[1.0, 1.1], [1.1, 1.2]])
+    eps_t = np.array([[1.0, 1.0], [1.0, 1.0]])
     sim.set_types(types)
-    sim.set_masses(masses=np.where(types == 0, 2.0, 1.0))
-    sim.set_pair_potential_parameters(sigma=np.array([[1.0, 1.1], [1.1, 1.2]]), epsilon=np.array([[1.0, 1.0],
-                                                                                                   [1.0, 1.0]]))
+    sim.set_masses(masses=masses)
+    sim.set_pair_potential_parameters(sigma=sig_t, epsilon=eps_t)
     sim.set_neighbor_list(skin=0.5, max_number_of_neighbors=256, method_str="cell list")
+    start = (np.array(sim.positions), np.array(sim.velocities), np.array(sim.image_positions),
+             np.array(sim.box_vectors))
     sim.run(warmup)
+    st0 = sim._stats()
     ms = sim.run_timed(steps)
+    rebuilds = int(sim._stats().rebuilds - st0.rebuilds)
     value = n * steps / (ms / 1000.0)
     bins = np.linspace(0.5, 3.5, 61)
     g = {}
     for a_t, b_t, key in ((0, 0, "AA"), (0, 1, "AB"), (1, 1, "BB")):
         r, gr = sim.get_radial_distribution_function(bins, type_a=a_t, type_b=b_t)
         g[key] = {"first_peak_r": float(r[np.argmax(gr)]), "first_peak_g": float(np.max(gr))}
-    return {"value": value, "unit": UNIT, "particles": n, "steps": steps, "ms_per_step": ms / steps,
-            "precision": "fp64 pair arithmetic, per-type sigma table", "T": sim.get_temperature(),
-            "U_per_particle": sim.get_potential_energy() / n, "g_r_first_peaks": g}
+    out = {"value": value, "unit": UNIT, "particles": n, "steps": steps, "ms_per_step": ms / steps,
+           "rebuilds_in_timed_region": rebuilds,
+           "precision": "fp64 pair arithmetic, per-type sigma table", "T": sim.get_temperature(),
+           "U_per_particle": sim.get_potential_energy() / n, "g_r_first_peaks": g}
+    del sim
+    out["cpu_baseline"] = wahnstrom_cpu(start, types, masses, sig_t, eps_t, seed, steps / max(rebuilds, 1))
+    return out
+
+
+def wahnstrom_cpu(start, types, masses, sig_t, eps_t, seed, gpu_steps_per_rebuild, max_seconds=12.0):
+    """The binary mixture on the host cores with the C port: per step skin
+    test, forces with sigma/epsilon per type pair, G-JF with the two masses,
+    wrap; rebuild (dompap's serial 3-D cell list) timed once and amortised."""
+    from oracle.cport import build as cport
+
+    pos, vel, img, box = (np.ascontiguousarray(a).copy() for a in start)
+    img = img.astype(np.int32)
+    n, dim = pos.shape
+    lib = cport.load()
+    fptr = cport.compile_potential("4*(r**-12-r**-6)", 2.5)
+    kmax = 256
+    nl = np.full((n, kmax), -1, dtype=np.int32)
+    beta, force = np.zeros_like(pos), np.zeros_like(pos)
+    mass = np.ascontiguousarray(masses, dtype=np.float64)
+    types = np.ascontiguousarray(types, dtype=np.int32)
+    sig = np.ascontiguousarray(sig_t, dtype=np.float64)
+    eps = np.ascontiguousarray(eps_t, dtype=np.float64)
+    scratch = np.zeros(n * dim)
+    ref_pos = pos.copy()
+    skin, cutoff = 0.5, float(np.max(sig_t)) * 2.5 + 0.5
+    lib.dp_port_seed(seed)
+
+    def P(a):
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+    def I(a):  # noqa: E743
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+    def rebuild():
+        lib.dp_port_nl_cell_list_3d(P(pos), n, P(box), cutoff, kmax, I(nl))
+        ref_pos[:] = pos
+
+    t0 = time.perf_counter()
+    rebuild()
+    t_build = time.perf_counter() - t0
+    done, rebuilds = 0, 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < max_seconds:
+        if lib.dp_port_nl_is_old(P(pos), P(ref_pos), n, dim, P(box), skin):
+            rebuild()
+            rebuilds += 1
+        lib.dp_port_forces_types(P(pos), n, dim, P(box), I(nl), kmax, fptr, I(types), sig.shape[0], P(sig), P(eps),
+                                 P(force))
+        lib.dp_port_gjf(P(pos), P(vel), P(beta), P(force), P(mass), n, dim, 0.004, 0.7, 0.2, P(scratch))
+        lib.dp_port_wrap(P(pos), I(img), n, dim, P(box))
+        done += 1
+    t = time.perf_counter() - t0
+    per_step = max((t - rebuilds * t_build) / done, 1e-12) + t_build / max(gpu_steps_per_rebuild, 1.0)
+    return {"value": n / per_step, "unit": UNIT, "cores": lib.dp_port_threads(), "kind": "port",
+            "sample": (f"{done} full steps of the same {n}-particle mixture on the host (C/OpenMP restatement of "
+                       f"dompap's loops, sigma/epsilon per type pair), rebuild {t_build:.2f} s amortised over "
+                       f"{gpu_steps_per_rebuild:.1f} steps/rebuild measured on the GPU")}
+
+
+def lj500_variant(seed, steps=10000, warmup=20):
+    """The reference's own CPU-runnable case (LJ fcc 5^3 = 500 at density
+    0.8442, T = 1, dt = 0.005, damping 0.1, skin 0.5, float64) for its stated
+    10,000 steps, beside the C port running the same 10,000 steps."""
+    sim = build_sim("lj500", seed)
+    n = sim.number_of_particles()
+    sim.run(warmup)
+    ms = sim.run_timed(steps)
+    lanes, blocks = sim.get_step_launch()
+    del sim
+    r = cpu_port_run("lj500", steps=steps, warmup=1, seed=seed, max_seconds=120.0)
+    cpu_value = r["n"] * r["steps"] / r["seconds"]
+    return {"value": n * steps / (ms / 1000.0), "unit": UNIT, "particles": n, "steps": steps,
+            "ms_per_step": ms / steps, "step_launch": {"lanes_per_particle": lanes, "ctas_per_sm": blocks},
+            "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": r["threads"], "kind": "port",
+                             "sample": (f"{r['steps']} full MD steps ({r['rebuilds']} rebuilds) of the same "
+                                        f"{r['n']}-particle system on the host, C/OpenMP restatement of "
+                                        "dompap's loops")}}
 
 
 def mlp_variant(seed, dim=3, steps=20, warmup=3, train_steps=100000):
@@ -592,6 +684,7 @@ def variant_table(args):
             ("batched_4096_lj", lambda: batched_variant(args.seed + 11)),
             ("harmonic2d", lambda: dimension_variant("harmonic2d", args.seed + 3, 500, 10)),
             ("harmonic4d", lambda: dimension_variant("harmonic4d", args.seed + 4, 300, 10)),
+            ("lj500_10000_steps", lambda: lj500_variant(args.seed + 9)),
             ("wahnstrom_256000", lambda: wahnstrom_variant(args.seed + 5)),
             ("mlp_surrogate_3d", lambda: mlp_variant(args.seed + 6, dim=3, train_steps=args.mlp_train_steps)),
             ("mlp_surrogate_4d", lambda: mlp_variant(args.seed + 8, dim=4, train_steps=args.mlp_train_steps)))
@@ -607,7 +700,45 @@ def variants(args, main_sim):
     return out
 
 
-def config_of(name, world=1):
+def profile_kernels(args):
+    """Launches for an ncu capture with ``--profile-from-start off``: the
+    workload's system brought to its melted state by ``run`` (untimed), then,
+    between cudaProfilerStart and cudaProfilerStop only, ``--profile-reps``
+    launches each of the list rebuild (cell binning, permutation into cell
+    order, Verlet build), the separate G-JF integrator, the fused step and the
+    separate force kernel (each after one warm-up launch, as dp_time_kernel
+    runs them), then as many training steps of the pair surrogate (batch
+    16,384, 2^20 samples of the costly potential). Prints the CUDA-event time
+    per launch of each."""
+    import torch
+
+    from dompap_gb300 import _lib
+    from dompap_gb300.mlp import PairSurrogate
+
+    torch.cuda.set_device(0)
+    sim = build_sim(args.workload, args.seed)
+    sim.run(MELT_STEPS)
+    sur = PairSurrogate(expensive_string(3.0), 3.0, r_min=0.8, n_samples=2 ** 20, seed=args.seed)
+    sur.train(steps=20)  # compiled and warm
+    lib = _lib.load()
+    torch.cuda.synchronize()
+    out = {}
+    ms = _lib.ctypes.c_float(0.0)
+    torch.cuda.profiler.start()
+    for name, which in (("rebuild", _lib.DP_KERNEL_REBUILD), ("gjf_integrate", _lib.DP_KERNEL_GJF),
+                        ("step", _lib.DP_KERNEL_STEP), ("forces", _lib.DP_KERNEL_FORCES)):
+        _lib.check(lib.dp_time_kernel(sim._h, which, args.profile_reps, _lib.ctypes.byref(ms)))
+        out[name] = float(ms.value)
+    t0 = time.perf_counter()
+    sur.train(steps=args.profile_reps)
+    torch.cuda.synchronize()
+    out["surrogate_training_step_host_ms"] = 1000 * (time.perf_counter() - t0) / args.profile_reps
+    torch.cuda.profiler.stop()
+    print(json.dumps({"profile_kernels_ms_per_launch": out, "workload": args.workload,
+                      "untimed_steps_before": MELT_STEPS}))
+
+
+def config_of(name, world=1, shuffle=False):
     """The workload's configuration, identical in both arms of the bench."""
     dim, unit, cells, rho, pot, rc, skin, T, dt, tau, jitter = WORKLOADS[name]
     n = int(np.prod(cells)) * len(unit)
@@ -615,7 +746,8 @@ def config_of(name, world=1):
             "density": rho, "pair_potential": pot, "r_cut": rc, "skin": skin, "temperature": T, "time_step": dt,
             "damping_time": tau, "jitter_sigma": jitter, "precision": "fp64 pair arithmetic",
             "l2": "working set > L2 (state + list ~ 0.3 GB for 1M particles, no flush)",
-            "parallelism": f"replicas x{world}" if world > 1 else "single system"}
+            "parallelism": f"replicas x{world}" if world > 1 else "single system",
+            **({"input_order": "particle ids randomly permuted"} if shuffle else {})}
 
 
 def step_roofline(sim, kt, name, state):
@@ -671,12 +803,21 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--mlp-train-steps", type=int, default=100000,
                     help="surrogate training steps (kernel timings do not depend on the weights)")
+    ap.add_argument("--shuffle-ids", action="store_true",
+                    help="randomly permute the particle ids of the input state (no spatial order)")
+    ap.add_argument("--profile-kernels", action="store_true",
+                    help="set up the melted system, then launch each kernel --profile-reps times between "
+                         "cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
+    ap.add_argument("--profile-reps", type=int, default=2)
     ap.add_argument("--only-variant", default=None,
                     help="run one variant of the full line alone and print its JSON (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.profile_kernels:
+        profile_kernels(args)
         return
     if args.only_variant:
         table = dict(variant_table(args))
@@ -702,7 +843,7 @@ def main():
         if dist is not None:
             dist.barrier()
 
-    sim = build_sim(args.workload, args.seed + rank)
+    sim = build_sim(args.workload, args.seed + rank, shuffle=args.shuffle_ids)
     n = sim.number_of_particles()
     sim.run(args.warmup)
     st0 = sim._stats()
@@ -729,7 +870,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": DATA,
-        "config": config_of(args.workload, world),
+        "config": config_of(args.workload, world, args.shuffle_ids),
         "clocks": clocks.summary(),
         "gpu_launches": launches,
         "e2e": {"value": e2e_total, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -759,7 +900,7 @@ def main():
         # the rebuild rate of the long melted window amortises the CPU port's rebuild
         steps_per_rebuild = line["melted"]["steps"] / max(line["melted"]["rebuilds_in_timed_region"], 1)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.workload, args.seed, steps_per_rebuild)
+        line["cpu_baseline"] = cpu_baseline(args.workload, args.seed, steps_per_rebuild, args.shuffle_ids)
     if rank == 0 and not args.no_variants:
         line["variants"] = variants(args, sim)
     if rank == 0:

@@ -25,6 +25,9 @@ DP_ERR_NONFINITE = 6
 DP_ERR_NOPOT = 7
 DP_ERR_TIMEOUT = 8
 
+DP_METHOD_LIST = 0
+DP_METHOD_ALLPAIRS = 1
+DP_METHOD_ALLPAIRS_NEWTON = 2
 DP_PREC_FP64 = 0
 DP_PREC_FP32 = 1
 DP_PREC_MLP = 2
@@ -125,6 +128,7 @@ _SIGNATURES = {
     "dp_time_forces": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "dp_kernel_launches": (ctypes.c_int64, [_P]),
     "dp_set_step_launch": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
+    "dp_set_pair_methods": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     "dp_get_step_launch": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "dp_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _I32, ctypes.POINTER(_P)]),
     "dp_batch_destroy": (ctypes.c_int, [_P]),

@@ -947,6 +947,8 @@ struct PairLib {
     cudaKernel_t step = nullptr;  // fused forces + integrate (not in the surrogate program)
     cudaKernel_t step_warp = nullptr;  // the same, one warp per particle (small systems)
     cudaKernel_t step_quad = nullptr;  // the same, four lanes per particle
+    // no neighbour list (dompap's double-loop methods): fused step, forces, energy
+    cudaKernel_t step_all = nullptr, forces_all = nullptr, energy_all = nullptr;
     cudaKernel_t batch[4] = {nullptr, nullptr, nullptr, nullptr};  // 128, 256, 512, 1024 threads
     cudaKernel_t forces_mlp = nullptr, energy_mlp = nullptr, virial_mlp = nullptr, mlp_finish = nullptr;
     cudaKernel_t forces_mlp_tc = nullptr, energy_mlp_tc = nullptr, virial_mlp_tc = nullptr;  // tcgen05
@@ -1106,6 +1108,9 @@ static int compile_pair_lib(const std::string& src, PairLib* out) {
         CK(cudaLibraryGetKernel(&pl.step, pl.lib, "dp_step"));
         CK(cudaLibraryGetKernel(&pl.step_warp, pl.lib, "dp_step_warp"));
         CK(cudaLibraryGetKernel(&pl.step_quad, pl.lib, "dp_step_quad"));
+        CK(cudaLibraryGetKernel(&pl.step_all, pl.lib, "dp_step_all"));
+        CK(cudaLibraryGetKernel(&pl.forces_all, pl.lib, "dp_forces_all"));
+        CK(cudaLibraryGetKernel(&pl.energy_all, pl.lib, "dp_energy_all"));
     }
     if (src.find("#define DP_MLP 1") != std::string::npos) {
         CK(cudaLibraryGetKernel(&pl.forces_mlp, pl.lib, "dp_forces_mlp"));
@@ -1159,6 +1164,12 @@ struct dp_sim {
     // CTAs per SM it is compiled for (0: the measured default per mode)
     int step_lanes = 0;
     int step_blocks = 0;
+    // force and energy methods (dompap's method strings): DP_METHOD_LIST or
+    // the all-pairs kernels (DP_METHOD_ALLPAIRS; DP_METHOD_ALLPAIRS_NEWTON for
+    // forces: parameters of each pair by (min, max) id). Not in the surrogate
+    // mode, whose kernels are list kernels.
+    int force_method = DP_METHOD_LIST;
+    int energy_method = DP_METHOD_LIST;
     // surrogate pass: 0 = tcgen05 from 65,536 particles (the 128-particle CTAs
     // fill the GPU; on par with mma.sync there), mma.sync below; 1 = tcgen05;
     // 2 = mma.sync (DOMPAP_MLP_TENSOR=tcgen05 | mma)
@@ -1665,6 +1676,15 @@ static int launch_pair(dp_sim* s, cudaKernel_t k, double* out, long long* launch
                                 fargs, 0, s->stream));
             if (launches) *launches += 1;
         }
+    } else if (k == s->lib.forces && s->force_method != DP_METHOD_LIST && s->lib.forces_all) {
+        a.upper = s->force_method == DP_METHOD_ALLPAIRS_NEWTON ? 1 : 0;
+        void* args[] = {&a};
+        CK(cudaLaunchKernel((const void*)s->lib.forces_all, dim3(grid_for(s->n * 32, kBlock)), dim3(kBlock), args, 0,
+                            s->stream));
+    } else if (k == s->lib.energy && s->energy_method != DP_METHOD_LIST && s->lib.energy_all) {
+        void* args[] = {&a};
+        CK(cudaLaunchKernel((const void*)s->lib.energy_all, dim3(grid_for(s->n * 32, kBlock)), dim3(kBlock), args, 0,
+                            s->stream));
     } else {
         void* args[] = {&a};
         CK(cudaLaunchKernel((const void*)k, dim3(grid_for(s->n, kBlock)), dim3(kBlock), args, 0, s->stream));
@@ -1903,6 +1923,11 @@ static bool use_fused_step(const dp_sim* s) {
     return s->fused_step && s->precision != DP_PREC_MLP && s->lib.step != nullptr;
 }
 
+// run() without a neighbour list: the all-pairs fused step
+static bool use_allpairs_step(const dp_sim* s) {
+    return use_fused_step(s) && s->force_method != DP_METHOD_LIST && s->lib.step_all != nullptr;
+}
+
 // The two position buffer sets change roles (host pointers only).
 static void swap_position_buffers(dp_sim* s) {
     std::swap(s->pos, s->pos_alt);
@@ -1921,6 +1946,13 @@ static int launch_step(dp_sim* s, int kind, long long step_offset, long long* la
     ia.shadow_out = s->shadow_alt;
     ia.pos64_out = s->pos64_alt;
     void* args[] = {&pa, &ia};
+    if (use_allpairs_step(s)) {
+        pa.upper = s->force_method == DP_METHOD_ALLPAIRS_NEWTON ? 1 : 0;
+        CK(cudaLaunchKernel((const void*)s->lib.step_all, dim3(grid_for(s->n * 32, kBlock)), dim3(kBlock), args, 0,
+                            s->stream));
+        if (launches) *launches += 1;
+        return DP_OK;
+    }
     const int lanes = s->step_lanes ? s->step_lanes
                                     : (s->n <= s->warp_step_max ? 32 : (s->n <= s->quad_step_max ? 4 : 1));
     if (lanes == 32 && s->lib.step_warp) {
@@ -1950,7 +1982,13 @@ static int record_steps(dp_sim* s, long long steps, int kind, cudaGraph_t graph,
         // after a fused step every position is wrapped: clear `far` before the
         // list check and the pair loop read it
         const bool reset_far = fused && t > 0;
-        if (conditional) {
+        if (use_allpairs_step(s)) {
+            // no list to keep: the step reads every particle's position
+            if (reset_far) {
+                k_clear_far<<<1, 1, 0, s->stream>>>(s->dstat);
+                *launches += 1;
+            }
+        } else if (conditional) {
             RET(capture_conditional_rebuild(s, graph, reset_far, launches, rebuild_launches));
         } else {
             if (reset_far) {
@@ -2125,7 +2163,7 @@ static int run_impl(dp_sim* s, long long steps, int kind, float* ms) {
         // a chunk needs the backup only if a list build inside it can
         // overflow: at a later step, or at its first step when a rebuild is
         // pending (hstat is current here)
-        const bool backed_up = c > 1 || s->hstat->need_rebuild != 0;
+        const bool backed_up = !use_allpairs_step(s) && (c > 1 || s->hstat->need_rebuild != 0);
         if (backed_up) RET(backup_state(s));
         GraphEntry* g = nullptr;
         RET(get_graph(s, c, kind, &g));
@@ -2547,6 +2585,20 @@ static int rebuild_pair_lib(dp_sim* s) {
     return DP_OK;
 }
 
+int dp_set_pair_methods(dp_sim* s, int force_method, int energy_method) {
+    if (!s) return fail(DP_ERR_ARG, "null handle");
+    if (force_method < DP_METHOD_LIST || force_method > DP_METHOD_ALLPAIRS_NEWTON)
+        return fail(DP_ERR_ARG, "unknown force method");
+    if (energy_method != DP_METHOD_LIST && energy_method != DP_METHOD_ALLPAIRS)
+        return fail(DP_ERR_ARG, "unknown energy method");
+    if (force_method != s->force_method || energy_method != s->energy_method) {
+        s->force_method = force_method;
+        s->energy_method = energy_method;
+        s->version++;
+    }
+    return DP_OK;
+}
+
 int dp_set_step_launch(dp_sim* s, int lanes, int blocks_per_sm) {
     if (!s) return fail(DP_ERR_ARG, "null handle");
     if (lanes != 0 && lanes != 1 && lanes != 4 && lanes != 32) return fail(DP_ERR_ARG, "lanes must be 0, 1, 4 or 32");
@@ -2766,7 +2818,8 @@ static int scalar_pair(dp_sim* s, cudaKernel_t k, double* out) {
     RET(update_nl(s, true, nullptr));
     // one partial sum per block of the kernel launch_pair uses
     const bool tc = s->precision == DP_PREC_MLP && use_mlp_tcgen05(s);
-    const long long blocks = grid_for(s->n, tc ? 128 : kBlock);
+    const bool all = k == s->lib.energy && s->energy_method != DP_METHOD_LIST && s->lib.energy_all;
+    const long long blocks = all ? grid_for(s->n * 32, kBlock) : grid_for(s->n, tc ? 128 : kBlock);
     RET(ensure_partial(s, blocks));
     RET(launch_pair(s, k, nullptr, nullptr));
     k_reduce<<<1, 1024, 0, s->stream>>>(s->partial, blocks, s->dsum);
@@ -2784,7 +2837,10 @@ static int scalar_pair(dp_sim* s, cudaKernel_t k, double* out) {
 int dp_potential_energy(dp_sim* s, double* energy) {
     double e = 0.0;
     RET(scalar_pair(s, s ? s->lib.energy : nullptr, &e));
-    *energy = e / 2;
+    // the list kernel sums every pair twice (dompap/potential.py:69-100 halves
+    // it); the double-loop kernel sums each pair once (:103-160)
+    const bool all = s->energy_method != DP_METHOD_LIST && s->lib.energy_all;
+    *energy = all ? e : e / 2;
     return DP_OK;
 }
 

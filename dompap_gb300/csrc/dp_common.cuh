@@ -50,7 +50,7 @@ struct dp_pair_args {
     dp_dev_status* status;
     long long n;
     int ntypes;
-    int pad0;
+    int upper;               // DP_PMODE == 2: parameters of (min, max) of the two ids (Newton's-third-law loop)
     double box[DP_MAX_DIM];
     float unit[DP_MAX_DIM];  // L / 2^32 per axis
     float unit64_hi[DP_MAX_DIM];  // L / 2^64 per axis as a double-float

@@ -56,8 +56,16 @@ __device__ __forceinline__ void dp_pair_params(const dp_pair_args& a, long long 
     isig = __ldg(a.isig_tab + ti * a.ntypes + tj);
     eps = __ldg(a.eps_tab + ti * a.ntypes + tj);
 #else
-    // the dense (N, N) tables are indexed by particle id
-    const long long pi = __ldg(a.order + i), pj = __ldg(a.order + j);
+    // the dense (N, N) tables are indexed by particle id; with `upper` by
+    // (min, max) of the two ids, as dompap's Newton's-third-law double loop
+    // (dompap/potential.py:191-214) evaluates every pair once with
+    // sigma(n, m), epsilon(n, m), n < m
+    long long pi = __ldg(a.order + i), pj = __ldg(a.order + j);
+    if (a.upper && pi > pj) {
+        const long long t = pi;
+        pi = pj;
+        pj = t;
+    }
     sig = __ldg(a.sig_tab + pi * a.n + pj);
     isig = 1.0 / sig;
     eps = __ldg(a.eps_tab + pi * a.n + pj);
@@ -65,7 +73,21 @@ __device__ __forceinline__ void dp_pair_params(const dp_pair_args& a, long long 
 }
 
 // What one kernel accumulates for a pair; selected at compile time.
-enum { DP_ACC_FORCE = 0, DP_ACC_ENERGY = 1, DP_ACC_VIRIAL = 2, DP_ACC_LAPLACE = 3 };
+// DP_ACC_ENERGY_UPPER: the energy over the partners m of n with m > n (ids).
+enum { DP_ACC_FORCE = 0, DP_ACC_ENERGY = 1, DP_ACC_VIRIAL = 2, DP_ACC_LAPLACE = 3, DP_ACC_ENERGY_UPPER = 4 };
+
+// The pair sum of particle (slot) i takes m > n in particle ids: the virial
+// (dompap/potential.py:265-278) and the double-loop energies (:103-160).
+// Per-type and constant parameters are symmetric, so any one orientation of
+// each pair gives the same total and slots are compared; the dense tables may
+// not be, so the ids are.
+__device__ __forceinline__ bool dp_upper_skip(const dp_pair_args& a, long long i, int j) {
+#if DP_PMODE == 2
+    return __ldg(a.order + j) <= __ldg(a.order + i);
+#else
+    return j <= i;
+#endif
+}
 
 // Per-particle neighbour loop. Returns the scalar sum (energy / virial /
 // Laplacian) and, for DP_ACC_FORCE, the force vector in f[].
@@ -81,7 +103,11 @@ enum { DP_ACC_FORCE = 0, DP_ACC_ENERGY = 1, DP_ACC_VIRIAL = 2, DP_ACC_LAPLACE = 
 // LANES > 1 (the fused step for small systems): LANES consecutive lanes share
 // particle i, lane `lane` of them taking list entries lane, lane + LANES, ...;
 // each returns its partial sums (the caller adds them across the group).
-template <int ACC, int LANES = 1>
+// ALL: no list, every other particle is a candidate partner (dompap's
+// double-loop and vectorised force and energy methods,
+// dompap/potential.py:103-160,191-250,298-324); lane `lane` takes slots
+// lane, lane + LANES, ...
+template <int ACC, int LANES = 1, bool ALL = false>
 __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long long i, double* f, int lane = 0) {
     constexpr int D = DP_DIM;
     const long long n = a.n;
@@ -137,19 +163,20 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
     // as often as its busiest lane has kept neighbours, not once per listed
     // one (in a dense liquid with a thin skin most listed neighbours of most
     // lanes are outside r_cut at any step).
-    const int c_all = a.cnt[i];
+    const int c_all = ALL ? (int)n : a.cnt[i];
     const int c = LANES > 1 ? (c_all > lane ? (c_all - lane + LANES - 1) / LANES : 0) : c_all;
-    const int32_t* __restrict__ row = a.nl + i + (LANES > 1 ? (long long)lane * n : 0LL);
+    const int32_t* __restrict__ row = ALL ? nullptr : a.nl + i + (LANES > 1 ? (long long)lane * n : 0LL);
     const long long entry_stride = (long long)LANES * n;
     for (int base = 0; base < c; base += 32) {
         const int w = min(32, c - base);
         uint32_t kept = 0;
 #pragma unroll 4
         for (int t = 0; t < w; ++t) {
-            const int j = __ldg(row + (long long)(base + t) * entry_stride);
-            // the virial is the reference's upper-triangle sum over n < m with
-            // sigma(n, m), epsilon(n, m) (dompap/potential.py:265-278)
-            if (ACC == DP_ACC_VIRIAL && j <= i) continue;
+            const int j = ALL ? (base + t) * LANES + lane : __ldg(row + (long long)(base + t) * entry_stride);
+            if (ALL && j == i) continue;
+            // the virial and the double-loop energy are upper-triangle sums
+            // over n < m with sigma(n, m), epsilon(n, m)
+            if ((ACC == DP_ACC_VIRIAL || ACC == DP_ACC_ENERGY_UPPER) && dp_upper_skip(a, i, j)) continue;
             uint32_t uj[D];
             dp_shadow_unpack<D>(__ldg(sh + j), uj);
             float df[D];
@@ -158,7 +185,7 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
         while (kept) {
             const int t = __ffs(kept) - 1;
             kept &= kept - 1;
-            const int j = __ldg(row + (long long)(base + t) * entry_stride);
+            const int j = ALL ? (base + t) * LANES + lane : __ldg(row + (long long)(base + t) * entry_stride);
             uint32_t uj[D];
 #if DP_FF
             unsigned long long Xj[D];
@@ -196,7 +223,7 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
                 const float g = sf * rinv;
 #pragma unroll
                 for (int k = 0; k < D; ++k) acc_v[k] = fmaf(g, df[k], acc_v[k]);
-            } else if (ACC == DP_ACC_ENERGY) {
+            } else if (ACC == DP_ACC_ENERGY || ACC == DP_ACC_ENERGY_UPPER) {
                 acc_s += (double)(e * dp_pair_u<float>(s, sinv));
             } else if (ACC == DP_ACC_VIRIAL) {
                 acc_s += (double)(e * dp_pair_f<float>(s, sinv) * r);
@@ -243,7 +270,7 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
 #endif
 #pragma unroll
                         for (int k = 0; k < D; ++k) dpff_accumulate_prod(facc[k], g, d[k]);
-                    } else if (ACC == DP_ACC_ENERGY) {
+                    } else if (ACC == DP_ACC_ENERGY || ACC == DP_ACC_ENERGY_UPPER) {
                         dpff_accumulate(sacc, feps * dp_pair_u<dpff>(s, sinv));
                     } else if (ACC == DP_ACC_VIRIAL) {
                         dpff_accumulate(sacc, feps * dp_pair_f<dpff>(s, sinv) * r);
@@ -297,7 +324,7 @@ __device__ __forceinline__ double dp_particle_sum(const dp_pair_args& a, long lo
                 const double g = sf * rinv;
 #pragma unroll
                 for (int k = 0; k < D; ++k) acc_v[k] = fma(g, d[k], acc_v[k]);
-            } else if (ACC == DP_ACC_ENERGY) {
+            } else if (ACC == DP_ACC_ENERGY || ACC == DP_ACC_ENERGY_UPPER) {
                 acc_s += eps * dp_pair_u<double>(s, sinv);
             } else if (ACC == DP_ACC_VIRIAL) {
                 acc_s += eps * dp_pair_f<double>(s, sinv) * r;
@@ -385,7 +412,7 @@ extern "C" __global__ void DP_STEP_BOUNDS dp_step(dp_pair_args a, dp_int_args b)
 // lane integrates. Below a few tens of thousands of particles this spreads the
 // pair loops over LANES times more threads than dp_step, whose one thread per
 // particle leaves most SMs idle.
-template <int LANES>
+template <int LANES, bool ALL = false>
 __device__ __forceinline__ void dp_step_split(const dp_pair_args& a, const dp_int_args& b) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long i = t / LANES;
@@ -395,7 +422,7 @@ __device__ __forceinline__ void dp_step_split(const dp_pair_args& a, const dp_in
     double f[DP_DIM];
 #pragma unroll
     for (int k = 0; k < DP_DIM; ++k) f[k] = 0.0;
-    if (active) dp_particle_sum<DP_ACC_FORCE, LANES>(a, i, f, lane);
+    if (active) dp_particle_sum<DP_ACC_FORCE, LANES, ALL>(a, i, f, lane);
     // every lane of the warp takes part in the shuffles (groups past the
     // last particle add zeros)
 #pragma unroll
@@ -418,6 +445,50 @@ __device__ __forceinline__ void dp_step_split(const dp_pair_args& a, const dp_in
 
 extern "C" __global__ void DP_STEP_BOUNDS dp_step_warp(dp_pair_args a, dp_int_args b) { dp_step_split<32>(a, b); }
 extern "C" __global__ void DP_STEP_BOUNDS dp_step_quad(dp_pair_args a, dp_int_args b) { dp_step_split<4>(a, b); }
+
+// ---------------------------------------------------------------------------
+// No neighbour list: dompap's double-loop and vectorised methods
+// (dompap/potential.py:103-160 energy, :191-250 and :298-324 forces). One
+// warp per particle; lane l takes the slots l, l + 32, ... (every other
+// particle is a candidate, tested with the same pre-filter and pair arithmetic
+// as the list kernels), and the partial sums are added across the warp in a
+// fixed order.
+extern "C" __global__ void DP_STEP_BOUNDS dp_step_all(dp_pair_args a, dp_int_args b) { dp_step_split<32, true>(a, b); }
+
+extern "C" __global__ void __launch_bounds__(256) dp_forces_all(dp_pair_args a) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long i = t >> 5;
+    const int lane = (int)(t & 31);
+    const bool active = i < a.n;  // uniform across the warp
+    double f[DP_DIM];
+#pragma unroll
+    for (int k = 0; k < DP_DIM; ++k) f[k] = 0.0;
+    if (active) dp_particle_sum<DP_ACC_FORCE, 32, true>(a, i, f, lane);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int k = 0; k < DP_DIM; ++k) f[k] += __shfl_down_sync(0xffffffffu, f[k], off);
+    }
+    if (!active || lane != 0) return;
+    bool finite = true;
+#pragma unroll
+    for (int k = 0; k < DP_DIM; ++k) {
+        a.out[k * a.n + i] = f[k];
+        finite = finite && dp_isfinite_bits(f[k]);
+    }
+    if (!finite) atomicExch(&a.status->nonfinite, 1);
+}
+
+// U = sum over n < m of eps u(r / sigma) (no halving), per-block partials.
+extern "C" __global__ void __launch_bounds__(256) dp_energy_all(dp_pair_args a) {
+    __shared__ double smem[32];
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long i = t >> 5;
+    double v = 0.0;
+    if (i < a.n) v = dp_particle_sum<DP_ACC_ENERGY_UPPER, 32, true>(a, i, nullptr, (int)(t & 31));
+    v = dp_block_sum(v, smem);
+    if (threadIdx.x == 0) a.partial[blockIdx.x] = v;
+}
 #endif
 
 // Per-block partial sums of a scalar pair quantity (energy or virial); the

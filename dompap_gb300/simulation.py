@@ -41,6 +41,13 @@ DEFAULT_NUMBER_OF_PARTICLES = 125
 _ALLPAIRS_LIMIT = 16384
 _DENSE_LIMIT = 8192
 
+# dompap's force / energy method strings -> the GPU kernels
+_FORCE_METHOD_CODES = {"neighbor list": _lib.DP_METHOD_LIST, "double loop": _lib.DP_METHOD_ALLPAIRS,
+                       "vectorized": _lib.DP_METHOD_ALLPAIRS,
+                       "double loop single core": _lib.DP_METHOD_ALLPAIRS_NEWTON}
+_ENERGY_METHOD_CODES = {"neighbor list": _lib.DP_METHOD_LIST, "double loop": _lib.DP_METHOD_ALLPAIRS,
+                        "double loop single core": _lib.DP_METHOD_ALLPAIRS}
+
 _STATE = ("positions", "velocities", "betas", "image_positions")
 _HOST_ONLY = ("masses", "particle_types", "box_vectors")
 
@@ -199,6 +206,7 @@ class Simulation:
         _lib.check(lib.dp_create(dim, n, create_prec, _lib.ctypes.byref(h)))
         d["_h"] = h
         d["_h_shape"] = (n, dim)
+        d["_methods_uploaded"] = None
         lanes, blocks = d.get("_step_launch", (0, 0))
         if lanes or blocks:
             _lib.check(lib.dp_set_step_launch(h, int(lanes), int(blocks)))
@@ -276,11 +284,22 @@ class Simulation:
             _lib.check(lib.dp_set_integrator(h, float(self.time_step), float(self.temperature_target),
                                              float(self.temperature_damping_time), d["_seed"] & (2**64 - 1)))
             d["_int_dirty"] = False
+        methods = self._pair_method_codes()
+        if d.get("_methods_uploaded") != methods:
+            _lib.check(lib.dp_set_pair_methods(h, *methods))
+            d["_methods_uploaded"] = methods
         if d.get("_nl_dirty"):
             method = self._nl_method_code()
             _lib.check(lib.dp_set_neighbor_list(h, float(self.neighbor_list_skin),
                                                 int(self.max_number_of_neighbors), method))
             d["_nl_dirty"] = False
+
+    def _pair_method_codes(self):
+        """dompap's force and energy method strings -> the GPU kernels
+        (neighbour-list kernels, or the all-pairs kernels for the double-loop
+        and vectorised methods, dompap/potential.py:103-160,191-250,298-324)."""
+        return (_FORCE_METHOD_CODES.get(self.force_method_str, _lib.DP_METHOD_LIST),
+                _ENERGY_METHOD_CODES.get(self.energy_method_str, _lib.DP_METHOD_LIST))
 
     def _nl_method_code(self):
         n = self.__dict__["_positions"].shape[0]

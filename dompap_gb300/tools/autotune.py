@@ -12,7 +12,9 @@ the GPU every force method is the same neighbour-list step kernel, so the
 candidates timed here are that kernel's launch shapes instead: one thread,
 four lanes or a warp per particle (the particle's list split over the lanes),
 then the resident CTAs per SM it is compiled for (4 or 6); the fastest is set
-on the system (``Simulation.set_step_launch``).
+on the system (``Simulation.set_step_launch``). With ``test_double_loop`` the
+step without a list (dompap's "double loop" force method: every pair, one
+warp per particle) is timed as well and chosen when it is faster.
 """
 from __future__ import annotations
 
@@ -92,8 +94,25 @@ def autotune(sim, steps=100, test_double_loop=True, smallest_skin=0.1, step_skin
         print(f"Fastest step launch: {best_shape[0]} lanes per particle, "
               f"{best_shape[1] if best_shape[1] else default_blocks} CTAs per SM")
     sim.set_step_launch(*best_shape)
+
+    # dompap's double-loop force method (autotune.py:112-128): no list, every
+    # pair evaluated (one warp per particle); kept when it beats the list step
+    method_times = {"neighbor list": shape_times[best_shape]}
+    if test_double_loop and n <= 65536:
+        sim_copy.set_step_launch(*best_shape)
+        sim_copy.force_method_str = "double loop"
+        sim_copy.run(steps)
+        method_times["double loop"] = min(sim_copy.run_timed(steps) for _ in range(2)) / 1000.0
+        sim_copy.force_method_str = "neighbor list"
+        if verbose:
+            print(f"Time with double loop: {method_times['double loop'] / steps * 1000:0.4f} milliseconds")
+    fastest_force = min(method_times, key=method_times.get)
+    sim.force_method_str = fastest_force
+    if verbose:
+        print(f"Fastest method: {sim.force_method_str}")
     sim.__dict__["_autotune_results"] = {"neighbor_list_build_s": results, "skins": skins, "skin_times_s": times,
-                                         "step_launch_times_s": shape_times, "step_launch": best_shape}
+                                         "step_launch_times_s": shape_times, "step_launch": best_shape,
+                                         "force_method_times_s": method_times, "force_method": fastest_force}
     if plot:
         try:
             import matplotlib.pyplot as plt

@@ -217,6 +217,22 @@ int dp_time_forces(dp_sim *sim, int reps, float *ms_per_launch);
 int dp_sum_mv2_noalloc(const double *velocities, const double *masses, int64_t n, int dim, double *out,
                        void *stream);
 
+/* Force and energy methods (dompap's method strings,
+ * dompap/Simulation.py:126-133 and the dispatch in get_forces :594-654 and
+ * get_potential_energy :545-592). DP_METHOD_LIST: the neighbour-list kernels
+ * ("neighbor list", dompap/potential.py:69-100,163-188). DP_METHOD_ALLPAIRS:
+ * no list, every pair evaluated ("double loop" and "vectorized" forces,
+ * potential.py:217-250,298-324: F_n = sum_m eps(n,m) f(r/sigma(n,m)) d/r;
+ * "double loop" energies, :103-160: U = sum_{n<m} eps(n,m) u(r/sigma(n,m))).
+ * DP_METHOD_ALLPAIRS_NEWTON (forces only): "double loop single core"
+ * (:191-214), every pair with the parameters of (min(n,m), max(n,m)); equal
+ * to the others unless sigma/epsilon are asymmetric callables. run() with an
+ * all-pairs force method keeps no list (the list is built on demand for the
+ * observables that use it). The surrogate mode always uses its list kernels. */
+#define DP_METHOD_LIST 0
+#define DP_METHOD_ALLPAIRS 1
+#define DP_METHOD_ALLPAIRS_NEWTON 2
+int dp_set_pair_methods(dp_sim *sim, int force_method, int energy_method);
 /* Launch shape of the fused step kernel, chosen by the autotuner
  * (dompap/tools/autotune.py:112-162 times dompap's force methods on the
  * actual system; here the candidates are launch shapes of the one GPU step):

@@ -51,6 +51,9 @@ def load():
     lib.dp_port_forces.restype = None
     lib.dp_port_forces.argtypes = [d, i64, ctypes.c_int, d, i32, ctypes.c_int, ctypes.c_void_p, ctypes.c_double,
                                    ctypes.c_double, d]
+    lib.dp_port_forces_types.restype = None
+    lib.dp_port_forces_types.argtypes = [d, i64, ctypes.c_int, d, i32, ctypes.c_int, ctypes.c_void_p, i32,
+                                         ctypes.c_int, d, d, d]
     lib.dp_port_gjf.restype = None
     lib.dp_port_gjf.argtypes = [d, d, d, d, d, i64, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, d]
     lib.dp_port_wrap.restype = None

@@ -11,6 +11,7 @@
  *                            cell width = cutoff, nc = ceil(L/cutoff) layout)
  *   dp_port_nl_is_old        dompap/neighbor_list.py:183-201  (serial)
  *   dp_port_forces           dompap/potential.py:163-188      (prange over n)
+ *   dp_port_forces_types     the same with sigma/epsilon per type pair
  *   dp_port_gjf              dompap/integrator.py:17-40       (vectorised NumPy, serial)
  *   dp_port_wrap             dompap/positions.py:90-98        (NumPy, serial)
  * Arrays are row-major (N, D) float64 as in dompap. The pair force is a
@@ -172,6 +173,34 @@ void dp_port_forces(const double *pos, int64_t n, int dim, const double *box, co
             }
             const double r = sqrt(q);
             const double sf = epsilon * f(r / sigma);
+            for (int c = 0; c < dim; ++c) acc[c] = acc[c] + sf * (d[c] / r);
+        }
+        for (int c = 0; c < dim; ++c) out[i * dim + c] = acc[c];
+    }
+}
+
+/* dp_port_forces with sigma(n, m), epsilon(n, m) from per-type tables
+ * (dompap/potential.py:163-188 calling its index callables sigma_func(n, m),
+ * epsilon_func(n, m), which the binary-mixture example makes table lookups by
+ * particle type: examples/wahnstrom_mixture.py:52-63). */
+void dp_port_forces_types(const double *pos, int64_t n, int dim, const double *box, const int32_t *nl, int kmax,
+                          pair_fn f, const int32_t *types, int ntypes, const double *sig_tab,
+                          const double *eps_tab, double *out) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const int ti = types[i];
+        for (int k = 0; k < kmax; ++k) {
+            const int32_t j = nl[i * kmax + k];
+            if (j == -1) break;
+            double d[8], q = 0.0;
+            for (int c = 0; c < dim; ++c) {
+                d[c] = min_image(pos[i * dim + c] - pos[(int64_t)j * dim + c], box[c]);
+                q += d[c] * d[c];
+            }
+            const double r = sqrt(q);
+            const int p = ti * ntypes + types[j];
+            const double sf = eps_tab[p] * f(r / sig_tab[p]);
             for (int c = 0; c < dim; ++c) acc[c] = acc[c] + sf * (d[c] / r);
         }
         for (int c = 0; c < dim; ++c) out[i * dim + c] = acc[c];

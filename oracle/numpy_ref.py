@@ -328,6 +328,46 @@ def forces_double_loop(positions, box_vectors, pair_force, sigma=1.0, epsilon=1.
     return forces
 
 
+def forces_double_loop_single_core(positions, box_vectors, pair_force, sigma=1.0, epsilon=1.0):
+    """``_get_forces_double_loop_single_core`` (dompap/potential.py:191-214):
+    each pair n < m once, with sigma(n, m), epsilon(n, m), added to n and
+    subtracted from m (Newton's third law), in the reference's loop order."""
+    pos = np.asarray(positions, dtype=np.float64)
+    box = np.asarray(box_vectors, dtype=np.float64)
+    n_part = pos.shape[0]
+    forces = np.zeros_like(pos)
+    for n in range(n_part - 1):
+        m_idx = np.arange(n + 1, n_part, dtype=np.int64)
+        d = _min_image(pos[n] - pos[m_idx], box)
+        dist = np.sum(d ** 2, axis=1) ** 0.5
+        sig = _pair_values(sigma, np.full(m_idx.size, n), m_idx)
+        eps = _pair_values(epsilon, np.full(m_idx.size, n), m_idx)
+        contrib = (eps * pair_force(dist / sig))[:, None] * (d / dist[:, None])
+        for k, m in enumerate(m_idx):
+            forces[n] = forces[n] + contrib[k]
+            forces[m] = forces[m] - contrib[k]
+    return forces
+
+
+def energy_double_loop(positions, box_vectors, pair_potential, sigma=1.0, epsilon=1.0) -> float:
+    """``_get_total_energy_double_loop`` (dompap/potential.py:103-130) and its
+    single-core twin (:133-160): sum over n < m of eps(n, m) u(r/sigma(n, m)),
+    not halved."""
+    pos = np.asarray(positions, dtype=np.float64)
+    box = np.asarray(box_vectors, dtype=np.float64)
+    n_part = pos.shape[0]
+    energy = 0.0
+    for n in range(n_part - 1):
+        m_idx = np.arange(n + 1, n_part, dtype=np.int64)
+        d = _min_image(pos[n] - pos[m_idx], box)
+        dist = np.sqrt(np.sum(d ** 2, axis=1))
+        sig = _pair_values(sigma, np.full(m_idx.size, n), m_idx)
+        eps = _pair_values(epsilon, np.full(m_idx.size, n), m_idx)
+        for t in eps * pair_potential(dist / sig).astype(np.float64):
+            energy = energy + t
+    return float(energy)
+
+
 # --------------------------------------------------------------------------
 # integrators  (dompap/integrator.py)
 # --------------------------------------------------------------------------

@@ -213,11 +213,51 @@ def make_rdf_types(rpos):
     print("golden_rdf_types.npz:", {k: float(np.max(out[k + "/g"])) for k in ("AA", "AB", "BB")})
 
 
+def make_methods(Simulation):
+    """The reference's own double-loop and vectorised force and energy
+    methods (dompap/potential.py:103-160,191-250,298-324, dispatched by
+    Simulation.get_forces / get_potential_energy) on configurations already in
+    ``golden_configs.npz``, rebuilt through the public setters: ``callable``
+    (asymmetric epsilon(n, m): the methods differ), ``wahn`` (per-type table)
+    and ``harm2d``."""
+    cfg = np.load(os.path.join(HERE, "golden_configs.npz"))
+    out = {}
+    for tag in ("callable", "wahn", "harm2d"):
+        c = {k.split("/", 1)[1]: cfg[k] for k in cfg.files if k.startswith(tag + "/")}
+        pos = np.array(c["positions"])
+        n, dim = pos.shape
+        sim = Simulation()
+        sim.positions = pos
+        sim.box_vectors = np.array(c["box"])
+        sim.velocities = np.array(c["velocities"])
+        sim.betas = np.zeros((n, dim))
+        sim.image_positions = np.zeros((n, dim), dtype=np.int32)
+        sim.masses = np.array(c["masses"]).reshape(-1, 1)
+        sim.particle_types = np.zeros((n, 1), dtype=np.int32)
+        sim.set_pair_potential(pair_potential_str=str(c["pot"]), r_cut=float(c["r_cut"]))
+        if "types" in c:
+            t, st, et = c["types"].reshape(-1), c["sigma_table"], c["epsilon_table"]
+            sim.set_pair_potential_parameters(sigma=lambda a, b: st[t[a], t[b]], epsilon=lambda a, b: et[t[a], t[b]])
+        elif "sigma_table" in c and np.ndim(c["sigma_table"]) == 2:
+            sm, em = c["sigma_table"], c["epsilon_table"]
+            sim.set_pair_potential_parameters(sigma=lambda a, b: sm[a, b], epsilon=lambda a, b: em[a, b])
+        sim.set_neighbor_list(skin=float(c["skin"]), max_number_of_neighbors=int(c["kmax"]))
+        for method in ("neighbor list", "double loop", "double loop single core", "vectorized"):
+            sim.force_method_str = method
+            out[f"{tag}/forces/{method}"] = np.array(sim.get_forces())
+        for method in ("neighbor list", "double loop", "double loop single core"):
+            sim.energy_method_str = method
+            out[f"{tag}/energy/{method}"] = np.float64(sim.get_potential_energy())
+        print(f"  {tag}: N={n}", flush=True)
+    np.savez_compressed(os.path.join(HERE, "golden_methods.npz"), **out)
+    print("golden_methods.npz:", len(out), "arrays")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("DOMPAP_REFERENCE"),
                     required="DOMPAP_REFERENCE" not in os.environ, help="path of an unmodified dompap 0.0.6 source tree (or set DOMPAP_REFERENCE)")
-    ap.add_argument("--only", choices=["checkpoint", "lammps", "rdf_types"], default=None,
+    ap.add_argument("--only", choices=["checkpoint", "lammps", "rdf_types", "methods"], default=None,
                     help="regenerate only the named fixture")
     args = ap.parse_args()
     dompap = import_reference(args.reference)
@@ -230,6 +270,11 @@ def main():
         from dompap import Simulation
 
         make_lammps(Simulation)
+        return
+    if args.only == "methods":
+        from dompap import Simulation
+
+        make_methods(Simulation)
         return
     if args.only == "rdf_types":
         from dompap import positions as rpos

@@ -47,6 +47,9 @@ def test_autotune_reference_case():
     assert lanes == best[0] and lanes in (1, 4, 32)
     assert blocks in (4, 6)
     assert set(k[0] for k in res["step_launch_times_s"]) == {1, 4, 32}  # 256 particles: all three timed
+    # dompap's force-method candidates: the list step and the double loop
+    assert set(res["force_method_times_s"]) == {"neighbor list", "double loop"}
+    assert sim.force_method_str == min(res["force_method_times_s"], key=res["force_method_times_s"].get)
     sim.run(200)
     assert np.all(np.isfinite(sim.positions))
 

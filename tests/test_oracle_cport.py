@@ -74,3 +74,27 @@ def test_gjf_without_noise_matches_the_oracle(lib, golden_unit):
                     _ptr(scratch))
     assert np.max(np.abs(pos - want[0])) <= 1e-14
     assert np.max(np.abs(vel - want[1])) <= 1e-14
+
+
+def test_type_table_forces_match_the_reference(lib, golden_configs):
+    """The binary mixture with sigma/epsilon per type pair (the reference's
+    index callables over a type table): forces to rounding."""
+    c = config_of(golden_configs, "wahn")
+    pos = np.ascontiguousarray(c["positions"], dtype=np.float64)
+    box = np.ascontiguousarray(c["box"], dtype=np.float64)
+    n, dim = pos.shape
+    kmax = int(c["kmax"])
+    types = np.ascontiguousarray(c["types"].reshape(-1), dtype=np.int32)
+    sig = np.ascontiguousarray(c["sigma_table"], dtype=np.float64)
+    eps = np.ascontiguousarray(c["epsilon_table"], dtype=np.float64)
+    cutoff = float(np.max(sig)) * float(c["r_cut"]) + float(c["skin"])
+    nl = np.empty((n, kmax), dtype=np.int32)
+    lib.dp_port_nl_double_loop(_ptr(pos), n, dim, _ptr(box), cutoff, kmax, _ptr(nl, ctypes.c_int32))
+    k = c["nlist"].shape[1]
+    assert np.array_equal(nl[:, :k], c["nlist"]) and np.all(nl[:, k:] == -1)
+    fptr = cport.compile_potential(str(c["pot"]), float(c["r_cut"]))
+    out = np.empty_like(pos)
+    lib.dp_port_forces_types(_ptr(pos), n, dim, _ptr(box), _ptr(nl, ctypes.c_int32), kmax, fptr,
+                             _ptr(types, ctypes.c_int32), sig.shape[0], _ptr(sig), _ptr(eps), _ptr(out))
+    want = c["forces"]
+    assert np.sqrt(np.mean((out - want) ** 2) / np.mean(want ** 2)) <= 1e-13

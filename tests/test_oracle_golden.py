@@ -230,3 +230,33 @@ def test_rdf_per_type_pair():
         r, g = ref.radial_distribution_function(pos[types == a], pos[types == b], box, gold["bins"])
         assert np.array_equal(r, gold[f"{key}/r"])
         np.testing.assert_allclose(g, gold[f"{key}/g"], rtol=1e-13, atol=0)
+
+
+def test_double_loop_methods():
+    """The oracle's double-loop force and energy methods against the
+    reference's own (dompap/potential.py:103-160,191-250,298-324), including
+    the asymmetric epsilon(n, m) where "double loop single core" (Newton's
+    third law with (n, m), n < m) and the upper-triangle energies differ from
+    the neighbour-list sums."""
+    from conftest import config_of, load_golden
+
+    gold = load_golden("golden_methods.npz")
+    cfgs = load_golden("golden_configs.npz")
+    for tag in ("callable", "wahn", "harm2d"):
+        c = config_of(cfgs, tag)
+        pos, box = c["positions"], c["box"]
+        u, f, _ = ref.make_pair_potential(str(c["pot"]), float(c["r_cut"]))
+        if "types" in c:
+            t = c["types"].reshape(-1)
+            sig, eps = c["sigma_table"][t[:, None], t[None, :]], c["epsilon_table"][t[:, None], t[None, :]]
+        elif "sigma_table" in c:
+            sig, eps = c["sigma_table"], c["epsilon_table"]
+        else:
+            sig, eps = 1.0, 1.0
+        for method, fn in (("double loop", ref.forces_double_loop),
+                           ("double loop single core", ref.forces_double_loop_single_core)):
+            want = gold[f"{tag}/forces/{method}"]
+            got = fn(pos, box, f, sig, eps)
+            assert np.sqrt(np.mean((got - want) ** 2) / np.mean(want ** 2)) <= 1e-13, (tag, method)
+        e = ref.energy_double_loop(pos, box, u, sig, eps)
+        assert abs(e - gold[f"{tag}/energy/double loop"]) <= 1e-12 * abs(gold[f"{tag}/energy/double loop"]), tag
