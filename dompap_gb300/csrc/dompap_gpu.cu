@@ -419,31 +419,46 @@ struct PermArgs {
     long long n;
 };
 
-__device__ __forceinline__ void copy_elem(const void* src, void* dst, long long from, long long to, int esize) {
-    switch (esize) {
-        case 1: ((uint8_t*)dst)[to] = ((const uint8_t*)src)[from]; break;
-        case 4: ((uint32_t*)dst)[to] = ((const uint32_t*)src)[from]; break;
-        case 8: ((uint2*)dst)[to] = ((const uint2*)src)[from]; break;
-        case 16: ((uint4*)dst)[to] = ((const uint4*)src)[from]; break;
-        default:
-            ((uint4*)dst)[2 * to] = ((const uint4*)src)[2 * from];
-            ((uint4*)dst)[2 * to + 1] = ((const uint4*)src)[2 * from + 1];
-            break;
+// Copy the components of one particle's entry: every load is issued before
+// the first store (independent loads in flight), element type by size.
+template <typename T>
+__device__ __forceinline__ void copy_comps(const void* src, void* dst, long long from, long long to, long long n,
+                                           int comps) {
+    T v[DP_MAX_DIM];
+#pragma unroll
+    for (int k = 0; k < DP_MAX_DIM; ++k)
+        if (k < comps) v[k] = ((const T*)src)[k * n + from];
+#pragma unroll
+    for (int k = 0; k < DP_MAX_DIM; ++k)
+        if (k < comps) ((T*)dst)[k * n + to] = v[k];
+}
+
+__device__ __forceinline__ void copy_entry(const PermArray& a, const void* src, void* dst, long long from,
+                                           long long to, long long n) {
+    switch (a.esize) {
+        case 1: copy_comps<uint8_t>(src, dst, from, to, n, a.comps); break;
+        case 4: copy_comps<uint32_t>(src, dst, from, to, n, a.comps); break;
+        case 8: copy_comps<uint2>(src, dst, from, to, n, a.comps); break;
+        case 16: copy_comps<uint4>(src, dst, from, to, n, 1); break;
+        default: {  // 32 bytes: two 16-byte halves
+            const uint4 lo = ((const uint4*)src)[2 * from], hi = ((const uint4*)src)[2 * from + 1];
+            ((uint4*)dst)[2 * to] = lo;
+            ((uint4*)dst)[2 * to + 1] = hi;
+        }
     }
 }
 
 // Gather every state array into cell order (into the scratch arrays) and
-// record the new slot of each particle id.
+// record the new slot of each particle id. One array per blockIdx.y, so the
+// arrays are copied side by side rather than one after another per thread.
 __global__ void k_permute(PermArgs p) {
     if (!p.st->need_rebuild) return;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.n) return;
     const long long o = p.src_of[t];
-    for (int q = 0; q < p.count; ++q) {
-        const PermArray& a = p.arr[q];
-        for (int k = 0; k < a.comps; ++k) copy_elem(a.data, a.scratch, k * p.n + o, k * p.n + t, a.esize);
-    }
-    p.slot_of[p.order[o]] = (int32_t)t;
+    const PermArray a = p.arr[blockIdx.y];
+    copy_entry(a, a.data, a.scratch, o, t, p.n);
+    if (blockIdx.y == 0) p.slot_of[p.order[o]] = (int32_t)t;
 }
 
 // The permuted copies back into the state arrays (the kernels captured after
@@ -452,10 +467,8 @@ __global__ void k_permute_back(PermArgs p) {
     if (!p.st->need_rebuild) return;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= p.n) return;
-    for (int q = 0; q < p.count; ++q) {
-        const PermArray& a = p.arr[q];
-        for (int k = 0; k < a.comps; ++k) copy_elem(a.scratch, a.data, k * p.n + t, k * p.n + t, a.esize);
-    }
+    const PermArray a = p.arr[blockIdx.y];
+    copy_entry(a, a.scratch, a.data, t, t, p.n);
 }
 
 __global__ void k_iota(int32_t* a, int32_t* b, long long n) {
@@ -495,7 +508,7 @@ struct NlArgs {
     double cutoff;
     float lo2;  // float32 r^2 below this: certainly inside the cutoff
     float hi2;  // float32 r^2 above this: certainly outside
-    int half;   // 1: partners j > i only (the surrogate mode's kernels use each pair once)
+    int half;   // 1: only the partners particle i owns (dp_owns_pair; the surrogate mode uses each pair once)
 };
 
 template <int D>
@@ -515,26 +528,41 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_cells(NlArgs a) {
     dp_shadow_unpack<D>(shi, ui);
     int ci[D];
     shadow_cell<D>(ui, a.nc, ci);
+    // each axis' share of the key for the cells at offsets -1, 0, +1 (periodic);
+    // a stencil cell's key is the sum of one share per axis (Morton: disjoint
+    // bits; row-major: coordinate times the axis stride)
+    int part[D][3];
+    {
+        int stride = 1;
+#pragma unroll
+        for (int k = D - 1; k >= 0; --k) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                int c = ci[k] + d - 1;
+                if (c < 0) c += a.nc[k];
+                if (c >= a.nc[k]) c -= a.nc[k];
+                part[k][d] = a.morton ? (int)(dp_spread_bits<D>((uint32_t)c) << (D - 1 - k)) : c * stride;
+            }
+            stride *= a.nc[k];
+        }
+    }
     int count = 0;
     int stencil = 1;
 #pragma unroll
     for (int k = 0; k < D; ++k) stencil *= 3;
     for (int s = 0; s < stencil; ++s) {
-        int cj[D];
+        int key = 0;
         int rem = s;
 #pragma unroll
         for (int k = D - 1; k >= 0; --k) {
-            int c = ci[k] + (rem % 3) - 1;
+            const int d = rem % 3;
             rem /= 3;
-            if (c < 0) c += a.nc[k];
-            if (c >= a.nc[k]) c -= a.nc[k];
-            cj[k] = c;
+            key += d == 0 ? part[k][0] : (d == 1 ? part[k][1] : part[k][2]);
         }
-        const int key = cell_key<D>(cj, a.nc, a.morton);
         const int lo = __ldg(a.bin_start + key), hi = __ldg(a.bin_start + key + 1);
         for (int t = lo; t < hi; ++t) {
             const int j = a.src_of ? __ldg(a.src_of + t) : t;
-            if (a.half ? j <= i : j == i) continue;
+            if (a.half ? !dp_owns_pair(i, j) : j == i) continue;
             // float32 pre-test on the fixed-point displacement (nearest image,
             // never longer than the single-shift one); float64 only near the cutoff
             uint32_t uj[D];
@@ -593,7 +621,7 @@ __global__ void __launch_bounds__(kBlock) k_nl_build_allpairs(NlArgs a) {
             const int lim = (int)min((long long)kBlock, n - base);
             for (int t = 0; t < lim; ++t) {
                 const long long j = base + t;
-                if (a.half ? j <= i : j == i) continue;
+                if (a.half ? !dp_owns_pair(i, j) : j == i) continue;
                 uint32_t uj[D];
                 dp_shadow_unpack<D>(tsh[t], uj);
                 float df[D];
@@ -660,7 +688,6 @@ __global__ void k_rebuild_cond(dp_dev_status* st, cudaGraphConditionalHandle h, 
     cudaGraphSetConditional(h, st->need_rebuild ? 1u : 0u);
 }
 
-__global__ void k_clear_far(dp_dev_status* st) { st->far = 0; }
 
 // End of a graph of steps; clear_far: its last (fused) step wrapped every position.
 __global__ void k_advance_step(dp_dev_status* st, long long steps, int clear_far) {
@@ -700,8 +727,9 @@ __global__ void k_nl_export(const int32_t* __restrict__ nl, const int32_t* __res
     for (int k = m; k < kout; ++k) row[k] = -1;
 }
 
-// A half list (partners j > i only) closed into the full one: row i gets its
-// own entries and i from every row j < i that holds it. The distance test is
+// A half list (each pair in the row of the particle that owns it,
+// dp_owns_pair) closed into the full one: row i gets its own entries and i
+// from every row j that holds it. The distance test is
 // symmetric (the min-image displacement of j - i is the negated one of i - j
 // and the sum of squares is the same), so the closure is the list a full
 // build at the same reference positions makes. Count pass, then scatter into
@@ -1174,8 +1202,9 @@ struct dp_sim {
     // fill the GPU; on par with mma.sync there), mma.sync below; 1 = tcgen05;
     // 2 = mma.sync (DOMPAP_MLP_TENSOR=tcgen05 | mma)
     int mlp_tensor = 0;
-    // neighbour lists hold partners j > i only in the surrogate mode (its
-    // kernels use each pair once); an export builds a full one for the moment
+    // neighbour lists hold only the partners a particle owns (dp_owns_pair)
+    // in the surrogate mode (its kernels use each pair once); an export
+    // builds a full one for the moment
     bool nl_half = false;         // kind of the list currently built
     // second set of position buffers: a fused step reads pos/shadow/pos64 and
     // writes these, then the two sets change roles
@@ -1496,7 +1525,7 @@ static void fill_perm_args(const dp_sim* s, PermArgs& p) {
 }
 
 // The gated rebuild sequence (no effect unless need_rebuild is set).
-// The surrogate mode uses each pair once: its lists hold the partners j > i only.
+// The surrogate mode uses each pair once: its lists hold only the partners a particle owns (dp_owns_pair).
 static bool list_half(const dp_sim* s) { return s->precision == DP_PREC_MLP; }
 
 static int launch_rebuild(dp_sim* s, long long* launches) {
@@ -1550,8 +1579,9 @@ static int launch_rebuild(dp_sim* s, long long* launches) {
             // the state into cell order: slot t <- slot src_of[t]
             PermArgs pa;
             fill_perm_args(s, pa);
-            k_permute<<<gp, kBlock, 0, s->stream>>>(pa);
-            k_permute_back<<<gp, kBlock, 0, s->stream>>>(pa);
+            const dim3 gpa(gp, (unsigned)pa.count);
+            k_permute<<<gpa, kBlock, 0, s->stream>>>(pa);
+            k_permute_back<<<gpa, kBlock, 0, s->stream>>>(pa);
             nl_launches += 2;
         }
         na.bin_start = s->bin_start;
@@ -1886,14 +1916,16 @@ static int update_nl(dp_sim* s, bool check, int* rebuilt) {
 // s->stream: a one-thread kernel sets the condition from need_rebuild, and the
 // body (captured on s->cstream) runs the cell and list kernels, so steps
 // without a rebuild launch none of them.
-static int capture_conditional_rebuild(dp_sim* s, cudaGraph_t graph, bool reset_far, long long* launches,
-                                       long long* body_launches) {
-    // a handle belongs to one conditional node: one per step
-    cudaGraphConditionalHandle h;
-    CK(cudaGraphConditionalHandleCreate(&h, graph, 0, 0));
-    k_rebuild_cond<<<1, 1, 0, s->stream>>>(s->dstat, h, reset_far ? 1 : 0);
-    CK(cudaGetLastError());
-    *launches += 1;
+// h: this step's handle (one per conditional node). With `set_cond` a
+// one-thread kernel sets its condition first; otherwise the previous fused
+// step's last CTA has set it (dp_step_end).
+static int capture_conditional_rebuild(dp_sim* s, cudaGraph_t graph, cudaGraphConditionalHandle h, bool set_cond,
+                                       bool reset_far, long long* launches, long long* body_launches) {
+    if (set_cond) {
+        k_rebuild_cond<<<1, 1, 0, s->stream>>>(s->dstat, h, reset_far ? 1 : 0);
+        CK(cudaGetLastError());
+        *launches += 1;
+    }
     cudaStreamCaptureStatus cs;
     const cudaGraphNode_t* deps = nullptr;
     size_t nd = 0;
@@ -1936,11 +1968,15 @@ static void swap_position_buffers(dp_sim* s) {
 }
 
 // Fused step: forces from the current buffers, integration into the others.
-static int launch_step(dp_sim* s, int kind, long long step_offset, long long* launches) {
+// end_flags / next_cond: DP_END_* work of the kernel's last CTA (graphs only).
+static int launch_step(dp_sim* s, int kind, long long step_offset, long long* launches, int end_flags = 0,
+                       cudaGraphConditionalHandle next_cond = 0) {
     dp_pair_args pa;
     fill_pair_args(s, pa, nullptr);
     dp_int_args ia;
     fill_int_args(s, ia, step_offset, kind);
+    ia.end_flags = end_flags;
+    ia.next_cond = next_cond;
     ia.force = nullptr;
     ia.pos_out = s->pos_alt;
     ia.shadow_out = s->shadow_alt;
@@ -1978,31 +2014,35 @@ static int launch_step(dp_sim* s, int kind, long long step_offset, long long* la
 static int record_steps(dp_sim* s, long long steps, int kind, cudaGraph_t graph, bool conditional, bool fused,
                         long long* launches, long long* rebuild_launches) {
     *rebuild_launches = 0;
+    const bool no_list = use_allpairs_step(s);
+    cudaGraphConditionalHandle h = 0;  // this step's rebuild node
+    if (conditional && !no_list) CK(cudaGraphConditionalHandleCreate(&h, graph, 0, 0));
     for (long long t = 0; t < steps; ++t) {
-        // after a fused step every position is wrapped: clear `far` before the
-        // list check and the pair loop read it
-        const bool reset_far = fused && t > 0;
-        if (use_allpairs_step(s)) {
+        // after a fused step every position is wrapped and `far` is clear (the
+        // step's last CTA clears it); the non-fused kernels clear it in
+        // k_integrate, before the next step's list check and pair loop
+        if (no_list) {
             // no list to keep: the step reads every particle's position
-            if (reset_far) {
-                k_clear_far<<<1, 1, 0, s->stream>>>(s->dstat);
-                *launches += 1;
-            }
         } else if (conditional) {
-            RET(capture_conditional_rebuild(s, graph, reset_far, launches, rebuild_launches));
+            // the condition of step t > 0 was set by the fused step t - 1
+            RET(capture_conditional_rebuild(s, graph, h, !fused || t == 0, false, launches, rebuild_launches));
         } else {
-            if (reset_far) {
-                k_clear_far<<<1, 1, 0, s->stream>>>(s->dstat);
-                *launches += 1;
-            }
             RET(launch_rebuild(s, launches));
         }
         if (fused) {
-            RET(launch_step(s, kind, t, launches));
+            cudaGraphConditionalHandle next = 0;
+            int flags = DP_END_CLEAR_FAR;
+            if (conditional && !no_list && t + 1 < steps) {
+                CK(cudaGraphConditionalHandleCreate(&next, graph, 0, 0));
+                flags |= DP_END_SET_COND;
+            }
+            RET(launch_step(s, kind, t, launches, flags, next));
             swap_position_buffers(s);
+            h = next;
         } else {
             RET(launch_pair(s, s->lib.forces, s->force, launches));
             RET(launch_integrate(s, kind, t, launches));
+            if (conditional && t + 1 < steps) CK(cudaGraphConditionalHandleCreate(&h, graph, 0, 0));
         }
     }
     k_advance_step<<<1, 1, 0, s->stream>>>(s->dstat, steps, fused && steps > 0 ? 1 : 0);

@@ -29,6 +29,9 @@ struct dp_dev_status {
     int32_t pad;
     int64_t rebuilds;         // neighbour-list builds done on the device
     int64_t step;             // steps integrated (the RNG counter)
+    // fused step in a graph: CTAs finished (low 32 bits) and CTAs with a
+    // particle beyond skin/2 (high 32 bits); its last CTA resets it
+    unsigned long long ticket;
 };
 
 // Arguments of the NVRTC-compiled pair kernels (pair_kernels.cuh); the host
@@ -198,6 +201,15 @@ __device__ __forceinline__ unsigned long long dp_fixed64_of(double p) {
     if (e >= 64) return ~0ull;
     const unsigned long long m = ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
     return e >= 52 ? m << (e - 52) : m >> (52 - e);
+}
+
+// Half lists (the surrogate mode evaluates each pair once): particle i owns
+// the pair {i, j} when the two slots differ in parity and i < j, or share it
+// and i > j. Exactly one of the two owns every pair, and each particle owns
+// about half of its partners whatever the order of the slots (the cell order
+// puts most partners of a particle early in a Morton block above it).
+__device__ __forceinline__ bool dp_owns_pair(long long i, long long j) {
+    return ((i ^ j) & 1) ? (i < j) : (i > j);
 }
 
 // x is neither infinite nor NaN (integer test of the exponent field).

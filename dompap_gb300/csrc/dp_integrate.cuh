@@ -43,7 +43,16 @@ struct dp_int_args {
     long long step_offset;       // steps since st->step (within one graph of steps)
     int massmode;                // 0: one mass, 1: mass classes, 2: per-particle masses
     int nve;                     // 1: NVE leap-frog, 0: G-JF
+    unsigned long long next_cond;  // fused step in a graph: conditional handle of the next step's rebuild node
+    int end_flags;               // fused step: DP_END_* work of its last CTA (0 outside graphs)
+    int pad_end;
 };
+
+// Work of the last CTA of a fused step captured in a graph: every position
+// is wrapped now, so `far` is cleared for the next step; and the next step's
+// conditional rebuild node gets its condition (need_rebuild) from here.
+#define DP_END_CLEAR_FAR 1
+#define DP_END_SET_COND 2
 
 // G-JF coefficients for mass m (dompap/integrator.py:29-36): a, b dt/m,
 // b/(2m), sqrt(2 alpha T dt), dt/m.

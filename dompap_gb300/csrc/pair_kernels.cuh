@@ -383,6 +383,30 @@ extern "C" __global__ void DP_FORCES_BOUNDS dp_forces(dp_pair_args a) {
 #ifndef DP_STEP_MIN_BLOCKS
 #define DP_STEP_MIN_BLOCKS 0
 #endif
+
+// Device-side condition of a graph's conditional node (CUDA device runtime).
+extern "C" __device__ void cudaGraphSetConditional(unsigned long long handle, unsigned int value);
+
+// End of a fused step in a graph. Each CTA adds 1 and, in the upper word, 1
+// if one of its particles moved beyond skin/2, to one 64-bit counter; the
+// CTA that brings the count to the grid size is the last one: every other CTA
+// has finished (and read `far`), so it clears `far` (all positions are
+// wrapped now) and sets the condition of the next step's rebuild node from
+// the summed flags, so that node needs no condition kernel of its own. No
+// fence is needed: the condition comes from the counter itself. Called by
+// every thread of the CTA with its own `old`.
+__device__ __forceinline__ void dp_step_end(const dp_int_args& b, bool old) {
+    if (b.end_flags == 0) return;  // uniform: launches outside graphs
+    const int cta_old = __syncthreads_or(old ? 1 : 0);
+    if (threadIdx.x != 0) return;
+    const unsigned long long mine = 1ull | ((unsigned long long)(cta_old != 0) << 32);
+    const unsigned long long prev = atomicAdd(&b.st->ticket, mine);
+    if ((unsigned)(prev & 0xffffffffull) != gridDim.x - 1) return;
+    b.st->ticket = 0ull;
+    const bool rebuild = ((prev + mine) >> 32) != 0;
+    if (b.end_flags & DP_END_CLEAR_FAR) b.st->far = 0;
+    if (b.end_flags & DP_END_SET_COND) cudaGraphSetConditional(b.next_cond, rebuild ? 1u : 0u);
+}
 #if DP_STEP_MIN_BLOCKS > 0
 #define DP_STEP_BOUNDS __launch_bounds__(256, DP_STEP_MIN_BLOCKS)
 #else
@@ -404,6 +428,7 @@ extern "C" __global__ void DP_STEP_BOUNDS dp_step(dp_pair_args a, dp_int_args b)
         if (any_old) atomicExch(&b.st->need_rebuild, 1);
         if (any_bad) atomicExch(&b.st->nonfinite, 1);
     }
+    dp_step_end(b, old);
 }
 
 // The fused step for small systems: LANES lanes per particle. The lanes
@@ -441,6 +466,7 @@ __device__ __forceinline__ void dp_step_split(const dp_pair_args& a, const dp_in
         if (any_old) atomicExch(&b.st->need_rebuild, 1);
         if (any_bad) atomicExch(&b.st->nonfinite, 1);
     }
+    dp_step_end(b, old);
 }
 
 extern "C" __global__ void DP_STEP_BOUNDS dp_step_warp(dp_pair_args a, dp_int_args b) { dp_step_split<32>(a, b); }
@@ -540,7 +566,7 @@ extern "C" __global__ void dp_eval_pair(const double* s_in, double* u, double* f
 // costly ones; sigma = epsilon = 1 in this mode. Each unique pair inside
 // r_cut is evaluated once (Newton's third law): a warp owns 32 particles, and
 // before each round every lane advances along its particle's neighbour list
-// to the next partner j > i inside r_cut, so a round's 32 network rows are
+// to the next partner it owns (dp_owns_pair) inside r_cut, so a round's 32 network rows are
 // all real pairs (two 16-row tensor-core tiles); each row's result goes back
 // to the lane owning the pair, which adds
 //   f/r = f_cheap(r)/r + (f r)_nn / r^2,   u = u_cheap(r) + u_nn.
@@ -597,7 +623,7 @@ __device__ __forceinline__ void dp_mlp_pass(const dp_pair_args& a, const dp_mlp_
         while (kk < c && !valid) {
             j = __ldg(a.nl + (long long)kk * n + i);
             ++kk;
-            if (j <= i) continue;
+            if (!dp_owns_pair(i, j)) continue;
             uint32_t uj[D];
             dp_shadow_unpack<D>(__ldg(sh + j), uj);
             const float qq = dp_shadow_q<D>(ui, uj, a.unit, df);
@@ -748,7 +774,7 @@ __device__ __forceinline__ void dp_mlp_pass_tc(const dp_pair_args& a, const dp_m
         while (kk < c && !nvalid) {
             const int jj = __ldg(a.nl + (long long)kk * n + i);
             ++kk;
-            if (jj <= i) continue;
+            if (!dp_owns_pair(i, jj)) continue;
             uint32_t uj[D];
             dp_shadow_unpack<D>(__ldg(sh + jj), uj);
             float dd[D];
