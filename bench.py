@@ -53,16 +53,24 @@ EXPENSIVE_RAW = "4*(r**-12-r**-6) + 0.5*exp(-(r-1.5)**2/0.02) + 0.1*cos(4*r)*exp
 BASIS_4D = ((0.0, 0.0, 0.0, 0.0), (0.5, 0.5, 0.0, 0.0), (0.0, 0.0, 0.5, 0.5), (0.5, 0.5, 0.5, 0.5))
 
 
-def expensive_string(r_cut=3.0):
-    """The costly test potential with its force shifted to zero at r_cut (the
-    smooth shift goes into the SymPy string; dompap only shifts the value)."""
+def extra_costly_terms(m):
+    """m more costly terms (a Gaussian bump times a cosine each) added to the
+    costly test potential, for the surrogate's crossover."""
+    return "".join(f" + 0.05*exp(-(r-{1.0 + 1.8 * k / max(m, 1):.4f})**2/0.05)*cos({3 + k}*r)" for k in range(m))
+
+
+def expensive_string(r_cut=3.0, extra_terms=0):
+    """The costly test potential (with ``extra_terms`` more costly terms) with
+    its force shifted to zero at r_cut (the smooth shift goes into the SymPy
+    string; dompap only shifts the value)."""
     import sympy as sp
 
     r = sp.symbols("r")
-    u = sp.sympify(EXPENSIVE_RAW)
+    raw = EXPENSIVE_RAW + extra_costly_terms(extra_terms)
+    u = sp.sympify(raw)
     u_rc = float(sp.N(u.subs(r, r_cut), 30))
     du_rc = float(sp.N(sp.diff(u, r).subs(r, r_cut), 30))
-    return f"{EXPENSIVE_RAW} - ({u_rc!r}) - (r - {float(r_cut)!r})*({du_rc!r})"
+    return f"{raw} - ({u_rc!r}) - (r - {float(r_cut)!r})*({du_rc!r})"
 
 
 def host_state(name, seed, shuffle=False):
@@ -373,7 +381,8 @@ def batched_variant(seed, steps=40, warmup=5, loop_sample=16):
     specs, rejected = lj_replica_specs(4096, seed)
     reps = Replicas(specs, "4*(r**-12-r**-6)", 2.5, time_step=0.005, damping_time=0.1, seed=seed)
     best, _ = reps.autotune(steps=5, candidates=[(1024, 128, 512), (1024, 256, 512), (2048, 256, 512),
-                                                  (512, 128, 256), (1024, 128, 256)])
+                                                  (512, 128, 256), (1024, 128, 256), (1024, 256, 1024),
+                                                  (2048, 256, 1024), (1024, 128, 1024)])
     reps.run(warmup)
     ms = reps.run(steps)
     value = reps.ntot * steps / (ms / 1000.0)
@@ -656,7 +665,34 @@ def mlp_variant(seed, dim=3, steps=20, warmup=3, train_steps=100000):
     res["unit"] = UNIT
     del sim
     res["nve_energy_drift"] = nve_drift_pair(sur, pot, dim, seed)
+    if dim == 3:
+        res["crossover"] = surrogate_crossover(res, seed, steps, warmup)
     return res
+
+
+def surrogate_crossover(res, seed, steps, warmup, extra=(0, 4, 8, 16, 32)):
+    """How costly a potential must be before the surrogate step beats the
+    float32 generated code: the surrogate's cost is the network's (the same for
+    any learned costly part), the generated code's grows with the terms it
+    evaluates. The costly test potential with m more costly terms, same
+    lattice (fcc 64^3, density 0.8), FP32 step time per m."""
+    from dompap_gb300.positions import FCC
+
+    sur_ms = res["surrogate"]["ms_per_step"]
+    rows = []
+    for m in extra:
+        pot = expensive_string(3.0, m)
+        sim = _lattice_sim(FCC, (64, 64, 64), 0.8, pot, 3.0, 0.3, 1.0, 0.004, 0.1, seed, 0.05, precision="fp32",
+                           kmax=256)
+        sim.run(warmup)
+        ms = sim.run_timed(steps) / steps
+        rows.append({"extra_costly_terms": m, "fp32_codegen_ms_per_step": ms})
+        del sim
+    faster = [r["extra_costly_terms"] for r in rows if r["fp32_codegen_ms_per_step"] > sur_ms]
+    return {"surrogate_ms_per_step": sur_ms, "fp32_codegen": rows,
+            "surrogate_faster_from_extra_terms": (min(faster) if faster else None),
+            "how": ("each extra term 0.05 exp(-(r - c)^2 / 0.05) cos(k r); the surrogate's step time is that of the "
+                    "network trained on the costly potential, which does not depend on the learned terms")}
 
 
 def nve_drift_pair(sur, pot, dim, seed, steps=1000, blocks=5):

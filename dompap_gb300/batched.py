@@ -117,14 +117,21 @@ class Replicas:
             candidates = [(s, ts, tl) for s, ts, tl in itertools.product((512, 1024, 2048), (128, 256), (256, 512))]
         best = None
         for cand in candidates:
-            self.set_launch(*cand)
-            self.run(steps)
-            t = self.run(steps)
+            try:
+                self.set_launch(*cand)
+                self.run(steps)
+                t = self.run(steps)
+            except _lib.DompapGPUError as exc:  # e.g. a CTA size this kernel cannot launch
+                if verbose:
+                    print(f"split_n={cand[0]:5d} threads_small={cand[1]:4d} threads_large={cand[2]:4d}: {exc}")
+                continue
             if verbose:
                 print(f"split_n={cand[0]:5d} threads_small={cand[1]:4d} threads_large={cand[2]:4d}: "
                       f"{t / steps:.4f} ms/step")
             if best is None or t < best[0]:
                 best = (t, cand)
+        if best is None:
+            raise _lib.DompapGPUError("no launch shape of the candidates ran")
         self.set_launch(*best[1])
         return best[1], best[0] / steps
 
