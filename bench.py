@@ -185,7 +185,7 @@ def measured_peaks():
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
 # measured by ncu on the named workload and state: "lattice" = the first steps
 # from the configuration's jittered lattice, "melted" = after MELT_STEPS steps
-PROFILED_TRAFFIC_BYTES = {("harmonic3d", "step", "melted"): 282.6e6}
+PROFILED_TRAFFIC_BYTES = {("harmonic3d", "step", "lattice"): 287.7e6, ("harmonic3d", "step", "melted"): 288.4e6}
 
 # untimed steps before the second ("melted") measurement of the headline
 # workload: the harmonic fcc lattice at T = 0.002 starts with its nearest
@@ -940,9 +940,10 @@ def main():
                           "rebuilds_in_timed_region": int(st1.rebuilds - st0.rebuilds),
                           "kernel_ms": mkt, "roofline": mroof}
     if dominant in ("forces", "step"):
-        line["roofline"]["note"] = ("float64-parity pair arithmetic runs in double-float on the FP32 pipes and "
-                                    "the neighbour gathers are dependent loads: the kernel is latency bound "
-                                    "(long-scoreboard stalls; DRAM 35 %, no pipe above 35 % under ncu)")
+        line["roofline"]["note"] = ("float64-parity pair arithmetic runs in double-float on the FP32 pipes, the "
+                                    "integrator's float64 on the 1/64-rate FP64 pipe, and the neighbour gathers are "
+                                    "dependent loads: the kernel is latency and issue bound (long-scoreboard "
+                                    "stalls, issue 56 %, FP64 pipe 33 %, DRAM 35 % under ncu)")
     if "melted" in line:
         # the rebuild rate of the long melted window amortises the CPU port's rebuild
         steps_per_rebuild = line["melted"]["steps"] / max(line["melted"]["rebuilds_in_timed_region"], 1)

@@ -2563,9 +2563,15 @@ static std::string hexd(double v) {
     return buf;
 }
 
+// step_sets_cond: the fused step may set the next step's graph condition
+// (device-side cudaGraphSetConditional); off for systems that run the gated
+// rebuild kernels instead of conditional nodes, whose step kernels profilers
+// can then follow inside graphs.
 static std::string pair_program(int dim, int precision, int pmode, bool sig_one, bool eps_one,
-                                const std::string& pot_src, bool with_batch, int step_blocks_hint = 6) {
+                                const std::string& pot_src, bool with_batch, int step_blocks_hint = 6,
+                                bool step_sets_cond = true) {
     std::string src;
+    src += std::string("#define DP_STEP_SETS_COND ") + (step_sets_cond ? "1" : "0") + "\n";
     src += "#define DP_DIM " + std::to_string(dim) + "\n";
     if (precision == DP_PREC_MLP) src += "#define DP_MLP 1\n";
     if (precision == DP_PREC_FP64) src += "#define DP_FF 1\n";
@@ -2616,7 +2622,8 @@ static int rebuild_pair_lib(dp_sim* s) {
     const bool eps_one = s->pmode == DP_PAIR_CONST && s->epsilon == 1.0;
     const int step_blocks = s->step_blocks ? s->step_blocks : step_blocks_for(s->dim, s->precision, s->pmode);
     const std::string src =
-        pair_program(s->dim, s->precision, s->pmode, sig_one, eps_one, s->pot_src, false, step_blocks);
+        pair_program(s->dim, s->precision, s->pmode, sig_one, eps_one, s->pot_src, false, step_blocks,
+                     s->conditional_graphs);
     PairLib pl;
     RET(compile_pair_lib(src, &pl));
     s->lib = pl;

@@ -384,8 +384,13 @@ extern "C" __global__ void DP_FORCES_BOUNDS dp_forces(dp_pair_args a) {
 #define DP_STEP_MIN_BLOCKS 0
 #endif
 
+#ifndef DP_STEP_SETS_COND
+#define DP_STEP_SETS_COND 1
+#endif
+#if DP_STEP_SETS_COND
 // Device-side condition of a graph's conditional node (CUDA device runtime).
 extern "C" __device__ void cudaGraphSetConditional(unsigned long long handle, unsigned int value);
+#endif
 
 // End of a fused step in a graph. Each CTA adds 1 and, in the upper word, 1
 // if one of its particles moved beyond skin/2, to one 64-bit counter; the
@@ -405,7 +410,11 @@ __device__ __forceinline__ void dp_step_end(const dp_int_args& b, bool old) {
     b.st->ticket = 0ull;
     const bool rebuild = ((prev + mine) >> 32) != 0;
     if (b.end_flags & DP_END_CLEAR_FAR) b.st->far = 0;
+#if DP_STEP_SETS_COND
     if (b.end_flags & DP_END_SET_COND) cudaGraphSetConditional(b.next_cond, rebuild ? 1u : 0u);
+#else
+    (void)rebuild;
+#endif
 }
 #if DP_STEP_MIN_BLOCKS > 0
 #define DP_STEP_BOUNDS __launch_bounds__(256, DP_STEP_MIN_BLOCKS)
