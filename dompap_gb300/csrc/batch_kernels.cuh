@@ -264,7 +264,10 @@ __device__ __forceinline__ void dp_batch_steps(const dp_batch_args& a) {
                     p = slot;
                     const int cnt = a.ncnt[off + p];
                     const uint16_t* __restrict__ row = nl + p;
-#pragma unroll 4
+                    // 16 list entries in flight per thread: the loop waits on the
+                    // list loads (4: 2.10e9, 8: 2.28e9, 16: 2.34e9, 24: 2.23e9, 32:
+                    // 2.09e9 particle-steps/s on 4,096 LJ replicas)
+#pragma unroll 16
                     for (int k = 0; k < cnt; ++k) pair(__ldg(row + (long long)k * n));
                 } else {
                     p = s_idx[slot];
