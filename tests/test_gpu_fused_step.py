@@ -75,3 +75,39 @@ def test_fused_step_is_the_run_kernel(monkeypatch, golden_configs):
         assert launches - 64 - per_rebuild * rebuilds == 2
     else:
         assert launches >= 64
+
+
+def test_prepared_graphs_with_odd_chunks_match_split_runs():
+    """run() captures every chunk graph it will launch before the first step,
+    each keyed by the position buffer set current when it starts (a fused chunk
+    of odd length leaves the other set current). 100,000 particles give chunks
+    of 41 steps: run(100) = 41 + 41 + 18 must give the same trajectory, bit for
+    bit, as run(41) followed by run(59) (the Langevin noise is keyed by step
+    and particle id, and the list rebuilds happen at the same steps)."""
+    from dompap_gb300 import Simulation
+    from dompap_gb300.positions import FCC
+
+    def system():
+        np.random.seed(77)  # the same seed for the noise of both systems
+        sim = Simulation()
+        sim.set_positions(unit_cell_coordinates=FCC, cells=(25, 25, 40), lattice_constants=(1.0, 1.0, 1.0))
+        sim.set_masses(masses=1.0)
+        sim.set_density(density=1.0)
+        rng = np.random.default_rng(5)
+        sim.positions = sim.positions + rng.normal(0.0, 0.05, size=sim.positions.shape)
+        sim.wrap_into_box()
+        sim.velocities = rng.normal(0.0, 0.3, size=sim.positions.shape)
+        sim.set_pair_potential("(1-r)**2", 1.0)
+        sim.set_neighbor_list(skin=0.2, max_number_of_neighbors=64, method_str="cell list")
+        sim.set_integrator(time_step=0.01, target_temperature=0.1, temperature_damping_time=0.1)
+        return sim
+
+    a, b = system(), system()
+    assert a.number_of_particles() == 100000
+    a.run(100)
+    b.run(41)
+    b.run(59)
+    assert a._stats().rebuilds == b._stats().rebuilds
+    assert np.array_equal(np.array(a.positions), np.array(b.positions))
+    assert np.array_equal(np.array(a.velocities), np.array(b.velocities))
+    assert np.array_equal(np.array(a.image_positions), np.array(b.image_positions))
