@@ -69,11 +69,12 @@ class PairSurrogate:
     """The trained network for the costly terms of one pair potential."""
 
     def __init__(self, pair_potential_str: str, r_cut: float, r_min: float = 0.8, n_samples: int = 2 ** 20,
-                 seed: int = 0, sampling: str = "uniform"):
+                 seed: int = 0, sampling: str = "uniform", init: str = "grid"):
         """Training samples r in [r_min, r_cut]: ``sampling`` "uniform" in r, or
         "pairs" with density proportional to r^(D-1) for D = 3 (uniform in r^3,
         as the pair distances of a homogeneous fluid), which weights the loss
-        as the pair sums (energy, virial) weigh the errors."""
+        as the pair sums (energy, virial) weigh the errors. ``init``: the
+        starting weights (``initial_params``)."""
         self.pair_potential_str = pair_potential_str
         self.r_cut = float(r_cut)
         self.r_min = float(r_min)
@@ -99,16 +100,48 @@ class PairSurrogate:
         _lib.check(lib.dp_mlp_create(ctypes.byref(h)))
         self._h = h
         self.nparam = int(lib.dp_mlp_param_count())
-        p = np.zeros(self.nparam, dtype=np.float32)
-        p[0:64] = rng.normal(0.0, 1.5, 64)
-        p[64:128] = rng.uniform(-2.0, 2.0, 64)
-        p[128:4224] = rng.normal(0.0, 1.0 / 8.0, 4096)
-        p[4288:4416] = rng.normal(0.0, 1.0 / 8.0, 128)
-        self.set_params(p)
+        if init not in ("grid", "random"):
+            raise ValueError(f"unknown init {init!r}")
+        self.init = init
+        self.set_params(self.initial_params(rng))
         _lib.check(lib.dp_mlp_set_data(h, _lib.fptr(np.ascontiguousarray(s, dtype=np.float32)),
                                        _lib.fptr(np.ascontiguousarray(targets)), n_samples))
         self.seed = seed
         self.losses = np.zeros(0, dtype=np.float32)
+
+    def initial_params(self, rng: np.random.Generator) -> np.ndarray:
+        """Starting weights. W2 and W3 ~ N(0, 1/8) (unit-variance
+        pre-activations over 64 inputs). Layer 1 with ``init`` "random": w1 ~
+        N(0, 1.5), b1 ~ U(-2, 2). With "grid": the 64 units are tanh steps
+        tanh(w (x - c)) whose centres c follow the density |d^2 (f r) / dx^2|^(1/3)
+        + 1/2 (relative to its mean) over the input range — the knot density
+        that minimises the error of a piecewise-linear fit, so more units sit
+        where the learned force bends — with slope w = 0.7 / (local spacing of
+        the centres) and a random sign. Measured on the costly test potential
+        (LJ + Gaussian + cos exp, r_cut 3, 100,000 Adam steps, seeds 0-3): force
+        RMS error on the 1M fcc lattice 0.73-1.2e-4 from the grid against
+        1.9-6.5e-4 from random starts; slopes 1 / spacing or steeper, and
+        centres spread evenly, fit worse."""
+        p = np.zeros(self.nparam, dtype=np.float32)
+        if self.init == "random":
+            p[0:64] = rng.normal(0.0, 1.5, 64)
+            p[64:128] = rng.uniform(-2.0, 2.0, 64)
+        else:
+            rg = np.linspace(self.r_min, self.r_cut, 4001)
+            _, f = _eval_codegen_fp64(self.costly_str, self.r_cut, rg)
+            x = (rg * rg - float(self.norm[0])) * float(self.norm[1])
+            y = f * rg
+            density = np.abs(np.gradient(np.gradient(y, x), x)) ** (1.0 / 3.0)
+            density = density / max(float(density.mean()), 1e-300) + 0.5
+            cdf = np.cumsum(density)
+            cdf = (cdf - cdf[0]) / (cdf[-1] - cdf[0])
+            centres = np.interp((np.arange(64) + 0.5) / 64, cdf, x)
+            w = 0.7 / np.gradient(centres) * np.where(rng.random(64) < 0.5, -1.0, 1.0)
+            p[0:64] = w
+            p[64:128] = -w * centres
+        p[128:4224] = rng.normal(0.0, 1.0 / 8.0, 4096)
+        p[4288:4416] = rng.normal(0.0, 1.0 / 8.0, 128)
+        return p
 
     # ------------------------------------------------------------- parameters
     def set_params(self, params: np.ndarray) -> None:
@@ -122,16 +155,70 @@ class PairSurrogate:
 
     # --------------------------------------------------------------- training
     def train(self, steps: int = 100000, batch: int = 16384, lr0: float = 2e-3, lr1: float = 1e-6, wf: float = 1.0,
-              accurate: bool = False) -> np.ndarray:
-        """Adam on the GPU; returns the minibatch loss of every step."""
+              accurate: bool = False, seed: int | None = None) -> np.ndarray:
+        """Adam on the GPU (minibatches drawn with ``seed``, by default the
+        constructor's); returns the minibatch loss of every step."""
+        seed = self.seed if seed is None else seed
         losses = np.empty(steps, dtype=np.float32)
         _lib.check(_lib.load().dp_mlp_train(self._h, int(steps), int(batch), float(lr0), float(lr1), float(wf),
-                                            int(self.seed) & (2 ** 64 - 1), int(bool(accurate)),
-                                            _lib.fptr(losses)))
+                                            int(seed) & (2 ** 64 - 1), int(bool(accurate)), _lib.fptr(losses)))
         self.losses = np.concatenate([self.losses, losses])
         return losses
 
+    def fit(self, steps: int = 100000, restarts: int = 3, judge=None, validation: int = 200000,
+            **train_kwargs) -> dict:
+        """``train`` from ``restarts`` starting points (the current weights,
+        then ``initial_params`` of further seeds) and keep the network the
+        judge prefers. ``judge``: a float64 ``Simulation`` of the potential —
+        the starts are ranked by their force error on its configuration against
+        the float64 generated code (``force_error``); without one, by the RMS
+        error of f/r on fresh samples uniform in r (a stream apart from the
+        training samples and from ``errors()``'s). The starts fit a narrow
+        feature unequally (the force error of a state spreads by up to 2x
+        between seeds), and the uniform-r error ranks them only loosely as the
+        force error in a system does. Returns each start's error and the index
+        kept; ``losses`` holds the kept start's."""
+        if restarts < 1:
+            raise ValueError("restarts must be >= 1")
+        reference = None if judge is None else self._judge_reference(judge)
+        best, tried, base = None, [], self.losses
+        for k in range(restarts):
+            if k > 0:
+                self.set_params(self.initial_params(np.random.default_rng([self.seed, k])))
+            self.losses = base
+            self.train(steps, seed=self.seed + k, **train_kwargs)
+            if judge is None:
+                err = self.errors(n=validation, seed=[self.seed, 2 ** 32 + k])["fr_rel_rms"]
+            else:
+                err = self.force_error(judge, reference)
+            tried.append(err)
+            if best is None or err < best[0]:
+                best = (err, k, self.params(), self.losses)
+        self.set_params(best[2])
+        self.losses = best[3]
+        return {"judge": "force_rel_rms" if judge is not None else "fr_rel_rms", "errors": tried, "kept": best[1]}
+
+    def _judge_reference(self, sim) -> np.ndarray:
+        if sim.__dict__["_precision"] not in (_lib.DP_PREC_FP64, _lib.DP_PREC_MLP):
+            raise ValueError("the judge runs the float64 generated code: set_precision('fp64')")
+        sim.set_pair_surrogate(None)
+        return sim.get_forces()
+
+    def force_error(self, sim, reference: np.ndarray | None = None) -> float:
+        """Relative RMS error of the forces on ``sim``'s configuration with
+        this network against the float64 generated code (``reference``: those
+        forces if already known); ``sim`` is left on the float64 code."""
+        f64 = self._judge_reference(sim) if reference is None else reference
+        sim.set_pair_surrogate(self)
+        try:
+            fnn = sim.get_forces()
+        finally:
+            sim.set_pair_surrogate(None)
+        return float(np.sqrt(np.mean((fnn - f64) ** 2) / np.mean(f64 ** 2)))
+
     def gradients(self, s: np.ndarray, targets: np.ndarray, wf: float = 1.0, accurate: bool = True):
+        """Loss and parameter gradient of one batch (the training kernels' own
+        forward and backward passes)."""
         s = np.ascontiguousarray(s, dtype=np.float32)
         t = np.ascontiguousarray(targets, dtype=np.float32)
         g = np.empty(self.nparam, dtype=np.float32)
@@ -154,7 +241,7 @@ class PairSurrogate:
         y = self.network(r ** 2).astype(np.float64)
         return y[:, 0] * float(self.norm[2]), y[:, 1] * float(self.norm[3]) / (r * r)
 
-    def errors(self, n: int = 200000, seed: int = 1) -> dict:
+    def errors(self, n: int = 200000, seed=1) -> dict:
         """Accuracy against the float64 generated code on fresh samples in
         [r_min, r_cut]: RMS errors of u and f/r of the costly terms, relative to
         the RMS of those terms, and relative to the total pair force f/r."""
