@@ -85,7 +85,8 @@ class Replicas:
     def set_neighbor_list(self, skin: float = 0.45, max_number_of_neighbors: int = 0) -> None:
         """Verlet lists per replica with partners within r_cut + skin (skin < 0:
         the 27-cell stencil every step); max_number_of_neighbors = 0 sizes them
-        from the densest replica."""
+        from the densest replica (a given capacity is rounded up to a multiple
+        of 8: the lists are stored in 8-entry chunks)."""
         _lib.check(_lib.load().dp_batch_set_neighbor_list(self._h, float(skin), int(max_number_of_neighbors)))
         self.skin = skin
 

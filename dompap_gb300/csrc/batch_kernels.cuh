@@ -10,7 +10,8 @@
 //      binning in shared memory — the fixed-point positions counting-sorted
 //      into cells at least r_cut + skin wide, or kept in index order when a
 //      box has fewer than 3 cells per axis (all pairs) — and a Verlet list per
-//      particle (16-bit local indices, column-major in HBM); a replica whose
+//      particle (16-bit local indices in 16-byte chunks of 8, the chunks
+//      column-major in HBM); a replica whose
 //      list would overflow its capacity uses the 27-cell stencil for the rest
 //      of the launch (binning every step), so no pair is ever missed;
 //   2. pair forces in float32 from the fixed-point displacements of the
@@ -54,6 +55,39 @@ __device__ __forceinline__ int dp_batch_block_scan(int* cnt, int nc, int* warp_t
     return carry;
 }
 
+// visit(q) for every binned slot q != slot of the (2 R + 1)^D cells around
+// the particle in `slot`. The stencil width is a compile-time constant, so the
+// digits of the stencil index are taken by multiplications, not divisions;
+// the first cell of the stencil is wrapped once per axis and each stencil cell
+// with a single conditional subtraction (a box has at least 2 R + 1 cells).
+template <int D, int R, typename Visit>
+__device__ __forceinline__ void dp_batch_stencil_cells(int slot, const uint32_t* up, const int* nc, const int* s_start,
+                                                       Visit& visit) {
+    constexpr int span = 2 * R + 1;
+    int stencil = 1;
+#pragma unroll
+    for (int k = 0; k < D; ++k) stencil *= span;
+    int lo[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        const int c = (int)__umulhi(up[k], (uint32_t)nc[k]) - R;
+        lo[k] = c < 0 ? c + nc[k] : c;
+    }
+    for (int s = 0; s < stencil; ++s) {
+        int rem = s, l = 0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            int cc = lo[k] + rem % span;
+            rem /= span;
+            cc -= (cc >= nc[k]) ? nc[k] : 0;
+            l = l * nc[k] + cc;
+        }
+        const int e = s_start[l + 1];
+        for (int q = s_start[l]; q < e; ++q)
+            if (q != slot) visit(q);
+    }
+}
+
 // visit(q) for every binned slot q != slot of the (2 reach + 1)^D cells
 // around the particle in `slot` (all slots when the box has no cells). Cells
 // are at least cutoff / reach wide, so the stencil covers the cutoff sphere.
@@ -61,27 +95,10 @@ template <int D, typename Visit>
 __device__ __forceinline__ void dp_batch_stencil(bool cells, int reach, int slot, const uint32_t* up, const int* nc,
                                                  const int* s_start, int n, Visit& visit) {
     if (cells) {
-        int cp[D];
-#pragma unroll
-        for (int k = 0; k < D; ++k) cp[k] = (int)__umulhi(up[k], (uint32_t)nc[k]);
-        const int span = 2 * reach + 1;
-        int stencil = 1;
-#pragma unroll
-        for (int k = 0; k < D; ++k) stencil *= span;
-        for (int s = 0; s < stencil; ++s) {
-            int rem = s, l = 0;
-#pragma unroll
-            for (int k = 0; k < D; ++k) {
-                int cc = cp[k] + (rem % span) - reach;
-                rem /= span;
-                cc += (cc < 0) ? nc[k] : 0;
-                cc -= (cc >= nc[k]) ? nc[k] : 0;
-                l = l * nc[k] + cc;
-            }
-            const int e = s_start[l + 1];
-            for (int q = s_start[l]; q < e; ++q)
-                if (q != slot) visit(q);
-        }
+        if (reach == 2)
+            dp_batch_stencil_cells<D, 2>(slot, up, nc, s_start, visit);
+        else
+            dp_batch_stencil_cells<D, 1>(slot, up, nc, s_start, visit);
     } else {
         for (int q = 0; q < n; ++q)
             if (q != slot) visit(q);
@@ -133,7 +150,7 @@ __device__ __forceinline__ void dp_batch_steps(const dp_batch_args& a) {
         for (int t = 0; t < 5; ++t) c[t] = a.coef[r * 5 + t];
         // the noise terms in float32, as the single-system integrator
         const float c2f = (float)c[2], c3f = (float)c[3];
-        // list of this replica: column-major, n rows
+        // list of this replica: chunk c of particle p at [(c n + p) 8]
         uint16_t* __restrict__ nl = a.nlist ? a.nlist + off * (long long)a.kmax : nullptr;
         bool use_list = nl != nullptr;  // cleared for the rest of the launch if the list overflows
 
@@ -206,7 +223,8 @@ __device__ __forceinline__ void dp_batch_steps(const dp_batch_args& a) {
                         dp_shadow_unpack<D>(s_sh[q], uq);
                         float df[D];
                         if (dp_shadow_q<D>(up, uq, unit, df) <= a.rl2) {
-                            if (cnt < a.kmax) nl[(long long)cnt * n + p] = s_idx[q];
+                            // 8-entry chunks: chunk c of particle p at [(c n + p) 8]
+                            if (cnt < a.kmax) nl[((long long)(cnt >> 3) * n + p) * 8 + (cnt & 7)] = s_idx[q];
                             ++cnt;
                         }
                     };
@@ -263,12 +281,23 @@ __device__ __forceinline__ void dp_batch_steps(const dp_batch_args& a) {
                 if (use_list) {
                     p = slot;
                     const int cnt = a.ncnt[off + p];
-                    const uint16_t* __restrict__ row = nl + p;
-                    // 16 list entries in flight per thread: the loop waits on the
-                    // list loads (4: 2.10e9, 8: 2.28e9, 16: 2.34e9, 24: 2.23e9, 32:
-                    // 2.09e9 particle-steps/s on 4,096 LJ replicas)
-#pragma unroll 16
-                    for (int k = 0; k < cnt; ++k) pair(__ldg(row + (long long)k * n));
+                    // one 16-byte load per 8 entries, two chunks ahead of the
+                    // pairs being evaluated
+                    const uint4* __restrict__ rowc = (const uint4*)nl + p;
+                    const int nch = (cnt + 7) >> 3;
+                    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+                    uint4 c1 = nch > 0 ? __ldg(rowc) : zero;
+                    uint4 c2 = nch > 1 ? __ldg(rowc + n) : zero;
+                    for (int ch = 0; ch < nch; ++ch) {
+                        const uint4 cur = c1;
+                        c1 = c2;
+                        c2 = ch + 2 < nch ? __ldg(rowc + (long long)(ch + 2) * n) : zero;
+                        const int m = cnt - 8 * ch;
+                        const uint32_t w[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+                        for (int e = 0; e < 8; ++e)
+                            if (e < m) pair((int)((w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu));
+                    }
                 } else {
                     p = s_idx[slot];
                     dp_batch_stencil<D>(cells, reach, slot, up, nc, s_start, n, pair);

@@ -3551,9 +3551,11 @@ int dp_batch_set_launch(dp_batch* b, int split_n, int threads_small, int threads
     return DP_OK;
 }
 
-// List capacity: 1.3 x the pair count of the densest replica's list sphere + 16.
+// List capacity: 1.3 x the pair count of the densest replica's list sphere +
+// 16, or the requested one; a multiple of 8 (the lists are stored in 8-entry
+// chunks of 16 bytes).
 static int batch_list_capacity(const dp_batch* b) {
-    if (b->kmax_req > 0) return std::min(b->kmax_req, 65535);
+    if (b->kmax_req > 0) return std::min((b->kmax_req + 7) & ~7, 65528);
     const double rl = b->r_cut + std::max(0.0, b->skin);
     const double pi = 3.141592653589793;
     const double sphere = b->dim == 2 ? pi * rl * rl : (b->dim == 3 ? 4.0 / 3.0 * pi * rl * rl * rl : 0.5 * pi * pi * rl * rl * rl * rl);
@@ -3564,7 +3566,7 @@ static int batch_list_capacity(const dp_batch* b) {
         rho = std::max(rho, (double)(b->h_offset[r + 1] - b->h_offset[r]) / vol);
     }
     const long long k = ((long long)std::ceil(1.3 * sphere * rho) + 16 + 7) & ~7LL;
-    return (int)std::min<long long>(std::max<long long>(k, 8), 65535);
+    return (int)std::min<long long>(std::max<long long>(k, 8), 65528);
 }
 
 static int batch_ensure_lists(dp_batch* b) {

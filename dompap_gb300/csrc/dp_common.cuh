@@ -97,7 +97,7 @@ struct dp_batch_args {
     int pad;
     unsigned long long seed;
     // Verlet lists (nlist == nullptr: cell stencil every step)
-    uint16_t* nlist;           // [off * kmax + k * n + p]: local index of the k-th listed neighbour of p
+    uint16_t* nlist;           // [off * kmax + ((k / 8) * n + p) * 8 + k % 8]: k-th listed neighbour of p
     int32_t* ncnt;             // [ntot] list lengths
     void* shadow_ref;          // [ntot] fixed-point positions at the replica's last build
     unsigned long long* list_stats;  // [0]: builds, [1]: replicas whose list overflowed
