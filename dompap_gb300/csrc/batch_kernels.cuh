@@ -56,35 +56,47 @@ __device__ __forceinline__ int dp_batch_block_scan(int* cnt, int nc, int* warp_t
 }
 
 // visit(q) for every binned slot q != slot of the (2 R + 1)^D cells around
-// the particle in `slot`. The stencil width is a compile-time constant, so the
-// digits of the stencil index are taken by multiplications, not divisions;
-// the first cell of the stencil is wrapped once per axis and each stencil cell
-// with a single conditional subtraction (a box has at least 2 R + 1 cells).
+// the particle in `slot`. Cells are numbered with the last axis fastest, so the
+// 2 R + 1 cells of a stencil row along it hold consecutive slots: the walk
+// takes (2 R + 1)^(D-1) rows, each one slot range (two where the row wraps
+// around the box). The stencil width is a compile-time constant, so the digits
+// of the row index are taken by multiplications, not divisions; a box has at
+// least 2 R + 1 cells per axis, so one conditional subtraction wraps a cell.
 template <int D, int R, typename Visit>
 __device__ __forceinline__ void dp_batch_stencil_cells(int slot, const uint32_t* up, const int* nc, const int* s_start,
                                                        Visit& visit) {
     constexpr int span = 2 * R + 1;
-    int stencil = 1;
+    int rows = 1;
 #pragma unroll
-    for (int k = 0; k < D; ++k) stencil *= span;
+    for (int k = 0; k + 1 < D; ++k) rows *= span;
     int lo[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) {
         const int c = (int)__umulhi(up[k], (uint32_t)nc[k]) - R;
         lo[k] = c < 0 ? c + nc[k] : c;
     }
-    for (int s = 0; s < stencil; ++s) {
-        int rem = s, l = 0;
+    const int nl = nc[D - 1];
+    const int a = lo[D - 1];         // first cell of a row along the last axis
+    const int b = a + 2 * R;         // last one, before the wrap
+    for (int s = 0; s < rows; ++s) {
+        int rem = s, base = 0;
 #pragma unroll
-        for (int k = 0; k < D; ++k) {
+        for (int k = 0; k + 1 < D; ++k) {
             int cc = lo[k] + rem % span;
             rem /= span;
             cc -= (cc >= nc[k]) ? nc[k] : 0;
-            l = l * nc[k] + cc;
+            base = base * nc[k] + cc;
         }
-        const int e = s_start[l + 1];
-        for (int q = s_start[l]; q < e; ++q)
+        base *= nl;
+        // cells a..b of the row (b < nl) or a..nl-1 and 0..b-nl
+        const int e1 = s_start[base + min(b, nl - 1) + 1];
+        for (int q = s_start[base + a]; q < e1; ++q)
             if (q != slot) visit(q);
+        if (b >= nl) {
+            const int e2 = s_start[base + (b - nl) + 1];
+            for (int q = s_start[base]; q < e2; ++q)
+                if (q != slot) visit(q);
+        }
     }
 }
 

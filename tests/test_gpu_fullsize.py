@@ -1,9 +1,11 @@
-"""The benchmark's own workload at full size: 1,048,576 particles (fcc 64^3 at
-density 1, N(0, 0.01) jitter, (1-r)^2 with r_cut = 1, skin 0.2, G-JF at
-T = 0.002) after 1000 steps. The neighbour rows of sampled particles equal the
-oracle's double loop over all particles (bit-exact pair sets at the list's
-reference positions), their forces equal the oracle's pair sums over those
-rows (1e-10 relative RMS), and the whole force field conserves momentum."""
+"""The benchmark's own workloads at full size: 1,048,576 particles at density
+1 with N(0, 0.01) jitter — fcc 64^3 (D = 3), the square lattice 1024^2 (D = 2)
+and the hypercubic lattice 32^4 (D = 4) — (1-r)^2 with r_cut = 1, skin 0.2,
+G-JF at T = 0.002, after 1000 steps. The neighbour rows of sampled particles
+equal the oracle's double loop over all particles (bit-exact pair sets at the
+list's reference positions), their forces equal the oracle's pair sums over
+those rows (1e-10 relative RMS), and the whole force field conserves
+momentum."""
 import numpy as np
 import pytest
 
@@ -12,17 +14,23 @@ from oracle import numpy_ref as ref
 pytestmark = pytest.mark.gpu
 
 R_CUT, SKIN = 1.0, 0.2
+LATTICES = {
+    2: (((0.0, 0.0),), (1024, 1024)),
+    3: (None, (64, 64, 64)),  # fcc
+    4: (((0.0, 0.0, 0.0, 0.0),), (32, 32, 32, 32)),
+}
 
 
-def _system():
+def _system(dim):
     from dompap_gb300 import Simulation
     from dompap_gb300.positions import FCC, generate_positions
 
-    cells = (64, 64, 64)
+    unit, cells = LATTICES[dim]
+    unit = FCC if unit is None else unit
     rng = np.random.default_rng(2024)
-    pos = generate_positions(FCC, cells, (1.0, 1.0, 1.0))
+    pos = generate_positions(unit, cells, (1.0,) * dim)
     box = np.array(cells, dtype=np.float64)
-    scale = (pos.shape[0] / np.prod(box)) ** (1 / 3)
+    scale = (pos.shape[0] / np.prod(box)) ** (1 / dim)
     box, pos = box * scale, pos * scale
     pos = pos + rng.normal(0.0, 0.01, size=pos.shape)
     img = np.floor(pos / box)
@@ -43,8 +51,9 @@ def _system():
     return sim
 
 
-def test_full_size_pair_sets_and_forces_against_oracle():
-    sim = _system()
+@pytest.mark.parametrize("dim", [2, 3, 4])
+def test_full_size_pair_sets_and_forces_against_oracle(dim):
+    sim = _system(dim)
     sim.run(1000)
     n = sim.number_of_particles()
     assert n == 1048576
@@ -57,7 +66,7 @@ def test_full_size_pair_sets_and_forces_against_oracle():
     cutoff = np.float64(1.0) * np.float64(R_CUT) + np.float64(SKIN)  # dompap/Simulation.py:353-356
     rng = np.random.default_rng(5)
     sample = rng.choice(n, size=200, replace=False)
-    want_f = np.zeros((sample.size, 3))
+    want_f = np.zeros((sample.size, dim))
     for k, i in enumerate(sample):
         # the pair set: get_neighbor_list_double_loop's test (dompap/neighbor_list.py:25-33) over all particles
         d = ref.displacement(ref_pos[i], ref_pos, box)
