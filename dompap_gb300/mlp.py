@@ -65,6 +65,23 @@ def _eval_codegen_fp64(pair_potential_str: str, r_cut: float, r: np.ndarray):
         lib.dp_destroy(h)
 
 
+def tanh_grid(x: np.ndarray, y: np.ndarray, rng: np.random.Generator, units: int = 64, slope: float = 0.7,
+              floor: float = 0.5):
+    """Layer-1 weights and biases (w, b) placing `units` tanh steps
+    tanh(w (x - c)) over the sampled input range x (increasing) of a target y:
+    centres c at the quantiles of |d^2 y / dx^2|^(1/3) + floor (relative to its
+    mean) — the knot density that minimises the error of a piecewise-linear
+    fit — each with slope `slope` / (local spacing of the centres) and a
+    random sign."""
+    density = np.abs(np.gradient(np.gradient(y, x), x)) ** (1.0 / 3.0)
+    density = density / max(float(density.mean()), 1e-300) + floor
+    cdf = np.cumsum(density)
+    cdf = (cdf - cdf[0]) / (cdf[-1] - cdf[0])
+    centres = np.interp((np.arange(units) + 0.5) / units, cdf, x)
+    w = slope / np.gradient(centres) * np.where(rng.random(units) < 0.5, -1.0, 1.0)
+    return w, -w * centres
+
+
 class PairSurrogate:
     """The trained network for the costly terms of one pair potential."""
 
@@ -130,15 +147,7 @@ class PairSurrogate:
             rg = np.linspace(self.r_min, self.r_cut, 4001)
             _, f = _eval_codegen_fp64(self.costly_str, self.r_cut, rg)
             x = (rg * rg - float(self.norm[0])) * float(self.norm[1])
-            y = f * rg
-            density = np.abs(np.gradient(np.gradient(y, x), x)) ** (1.0 / 3.0)
-            density = density / max(float(density.mean()), 1e-300) + 0.5
-            cdf = np.cumsum(density)
-            cdf = (cdf - cdf[0]) / (cdf[-1] - cdf[0])
-            centres = np.interp((np.arange(64) + 0.5) / 64, cdf, x)
-            w = 0.7 / np.gradient(centres) * np.where(rng.random(64) < 0.5, -1.0, 1.0)
-            p[0:64] = w
-            p[64:128] = -w * centres
+            p[0:64], p[64:128] = tanh_grid(x, f * rg, rng)
         p[128:4224] = rng.normal(0.0, 1.0 / 8.0, 4096)
         p[4288:4416] = rng.normal(0.0, 1.0 / 8.0, 128)
         return p
