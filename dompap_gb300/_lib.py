@@ -125,7 +125,6 @@ _SIGNATURES = {
                                      ctypes.POINTER(ctypes.c_uint64)]),
     "dp_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(DpStats)]),
     "dp_time_kernel": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
-    "dp_time_forces": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "dp_kernel_launches": (ctypes.c_int64, [_P]),
     "dp_set_step_launch": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     "dp_set_pair_methods": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),

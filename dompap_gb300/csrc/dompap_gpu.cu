@@ -3030,7 +3030,6 @@ int dp_time_kernel(dp_sim* s, int which, int reps, float* ms) {
     return DP_OK;
 }
 
-int dp_time_forces(dp_sim* s, int reps, float* ms) { return dp_time_kernel(s, DP_KERNEL_FORCES, reps, ms); }
 
 int dp_wrap(dp_sim* s) {
     if (!s) return fail(DP_ERR_ARG, "null handle");

@@ -193,8 +193,6 @@ int dp_get_stats(dp_sim *sim, dp_stats *stats);
  * current state (ms per launch, CUDA events on the handle's stream). The
  * integrator variants advance the state; the list is rebuilt afterwards. */
 int dp_time_kernel(dp_sim *sim, int which, int reps, float *ms_per_launch);
-/* dp_time_kernel(sim, DP_KERNEL_FORCES, reps, ms_per_launch). */
-int dp_time_forces(dp_sim *sim, int reps, float *ms_per_launch);
 /* sum_n m_n |v_n|^2 like dp_sum_mv2, but on caller-owned device arrays and
  * without allocating anything; it has no counterpart in the reference.
  * For callers that cannot call cudaMalloc: hosts that hand out all device
