@@ -630,16 +630,16 @@ def mlp_variant(seed, dim=3, steps=20, warmup=3, train_steps=100000, restarts=3)
     pot = expensive_string(3.0)
     t0 = time.perf_counter()
     unit, cells = (FCC, (64, 64, 64)) if dim == 3 else (BASIS_4D, (16, 16, 16, 16))
-    judge_cells = (24, 24, 24) if dim == 3 else (10, 10, 10, 10)
+    rank_cells = (24, 24, 24) if dim == 3 else (10, 10, 10, 10)
     sur = PairSurrogate(pot, 3.0, r_min=0.8, n_samples=2 ** 20, seed=seed)
     # the starts are ranked on an independent configuration of the same state
     # (smaller, other noise seed); the error below is measured on the benchmark's
-    judge = _lattice_sim(unit, judge_cells, 0.8, pot, 3.0, 0.3, 1.0, 0.004, 0.1, seed + 1000, 0.05,
-                         kmax=256 if dim == 3 else 512)
-    starts = sur.fit(steps=train_steps, restarts=restarts, judge=judge)
-    starts["judge_state"] = (f"{'fcc' if dim == 3 else '4-point'} {'x'.join(map(str, judge_cells))} cells, density "
-                             "0.8, N(0, 0.05) jitter from another seed")
-    del judge
+    rank_sim = _lattice_sim(unit, rank_cells, 0.8, pot, 3.0, 0.3, 1.0, 0.004, 0.1, seed + 1000, 0.05,
+                            kmax=256 if dim == 3 else 512)
+    starts = sur.fit(steps=train_steps, restarts=restarts, rank_on=rank_sim)
+    starts["ranked_on"] = (f"{'fcc' if dim == 3 else '4-point'} {'x'.join(map(str, rank_cells))} cells, density "
+                           "0.8, N(0, 0.05) jitter from another seed")
+    del rank_sim
     losses = sur.losses
     t_train = time.perf_counter() - t0
     acc = sur.errors()

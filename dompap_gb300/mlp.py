@@ -174,11 +174,11 @@ class PairSurrogate:
         self.losses = np.concatenate([self.losses, losses])
         return losses
 
-    def fit(self, steps: int = 100000, restarts: int = 3, judge=None, validation: int = 200000,
+    def fit(self, steps: int = 100000, restarts: int = 3, rank_on=None, validation: int = 200000,
             **train_kwargs) -> dict:
         """``train`` from ``restarts`` starting points (the current weights,
         then ``initial_params`` of further seeds) and keep the network the
-        judge prefers. ``judge``: a float64 ``Simulation`` of the potential —
+        float64 generated code prefers. ``rank_on``: a float64 ``Simulation`` of the potential —
         the starts are ranked by their force error on its configuration against
         the float64 generated code (``force_error``); without one, by the RMS
         error of f/r on fresh samples uniform in r (a stream apart from the
@@ -189,27 +189,28 @@ class PairSurrogate:
         kept; ``losses`` holds the kept start's."""
         if restarts < 1:
             raise ValueError("restarts must be >= 1")
-        reference = None if judge is None else self._judge_reference(judge)
+        reference = None if rank_on is None else self._fp64_forces(rank_on)
         best, tried, base = None, [], self.losses
         for k in range(restarts):
             if k > 0:
                 self.set_params(self.initial_params(np.random.default_rng([self.seed, k])))
             self.losses = base
             self.train(steps, seed=self.seed + k, **train_kwargs)
-            if judge is None:
+            if rank_on is None:
                 err = self.errors(n=validation, seed=[self.seed, 2 ** 32 + k])["fr_rel_rms"]
             else:
-                err = self.force_error(judge, reference)
+                err = self.force_error(rank_on, reference)
             tried.append(err)
             if best is None or err < best[0]:
                 best = (err, k, self.params(), self.losses)
         self.set_params(best[2])
         self.losses = best[3]
-        return {"judge": "force_rel_rms" if judge is not None else "fr_rel_rms", "errors": tried, "kept": best[1]}
+        return {"ranked_by": "force_rel_rms" if rank_on is not None else "fr_rel_rms", "errors": tried,
+                "kept": best[1]}
 
-    def _judge_reference(self, sim) -> np.ndarray:
+    def _fp64_forces(self, sim) -> np.ndarray:
         if sim.__dict__["_precision"] not in (_lib.DP_PREC_FP64, _lib.DP_PREC_MLP):
-            raise ValueError("the judge runs the float64 generated code: set_precision('fp64')")
+            raise ValueError("the ranking runs the float64 generated code: set_precision('fp64')")
         sim.set_pair_surrogate(None)
         return sim.get_forces()
 
@@ -217,7 +218,7 @@ class PairSurrogate:
         """Relative RMS error of the forces on ``sim``'s configuration with
         this network against the float64 generated code (``reference``: those
         forces if already known); ``sim`` is left on the float64 code."""
-        f64 = self._judge_reference(sim) if reference is None else reference
+        f64 = self._fp64_forces(sim) if reference is None else reference
         sim.set_pair_surrogate(self)
         try:
             fnn = sim.get_forces()

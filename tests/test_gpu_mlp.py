@@ -28,9 +28,9 @@ def surrogate():
 
     sur = PairSurrogate(expensive_string(), 3.0, r_min=0.8, n_samples=2 ** 20, seed=0)
     # ranked on a small lattice of another noise seed than the target test's
-    starts = sur.fit(steps=100000, restarts=3, judge=_jittered_fcc((16, 16, 16), seed=7), batch=16384, lr0=2e-3,
+    starts = sur.fit(steps=100000, restarts=3, rank_on=_jittered_fcc((16, 16, 16), seed=7), batch=16384, lr0=2e-3,
                      lr1=1e-6)
-    print("force errors of the starts on the judge's lattice:", starts)
+    print("force errors of the starts on the ranking lattice:", starts)
     return sur
 
 
