@@ -62,3 +62,25 @@ def test_reference_arm_runs_on_rank_zero_only():
                          capture_output=True, text=True, env=env, timeout=300)
     assert res.returncode == 0, res.stderr
     assert res.stdout.strip() == ""
+
+
+def test_reference_arm_line_on_rank_zero():
+    """The reference arm's JSON line (dompap's loops restated in C, on the host
+    cores) on the small workload: the contract's keys, and the same `config`
+    as the repo's own arm."""
+    import json
+
+    sys.path.insert(0, REPO)
+    import bench
+
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    res = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--workload", "lj500",
+                          "--steps", "2", "--warmup", "3"], capture_output=True, text=True, env=env, timeout=300)
+    assert res.returncode == 0, res.stderr
+    line = json.loads(res.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["value"] > 0 and line["steps"] == 2 and line["higher_is_better"] is True
+    assert line["config"] == bench.config_of("lj500", 1, False)
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": bench.UNIT, "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
