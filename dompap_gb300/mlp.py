@@ -177,16 +177,16 @@ class PairSurrogate:
     def fit(self, steps: int = 100000, restarts: int = 3, rank_on=None, validation: int = 200000,
             **train_kwargs) -> dict:
         """``train`` from ``restarts`` starting points (the current weights,
-        then ``initial_params`` of further seeds) and keep the network the
-        float64 generated code prefers. ``rank_on``: a float64 ``Simulation`` of the potential —
-        the starts are ranked by their force error on its configuration against
-        the float64 generated code (``force_error``); without one, by the RMS
-        error of f/r on fresh samples uniform in r (a stream apart from the
-        training samples and from ``errors()``'s). The starts fit a narrow
-        feature unequally (the force error of a state spreads by up to 2x
-        between seeds), and the uniform-r error ranks them only loosely as the
-        force error in a system does. Returns each start's error and the index
-        kept; ``losses`` holds the kept start's."""
+        then ``initial_params`` of further seeds) and keep the best network.
+        ``rank_on``: a float64 ``Simulation`` of the potential — the starts are
+        ranked by their force error on its configuration against the float64
+        generated code (``force_error``); without one, by the RMS error of f/r
+        on fresh samples uniform in r (a stream apart from the training samples
+        and from ``errors()``'s). The starts fit a narrow feature unequally (the
+        force error of a state spreads by up to 2x between seeds), and the
+        uniform-r error ranks them only loosely as the force error in a system
+        does. Returns each start's error and the index kept; ``losses`` holds
+        the kept start's."""
         if restarts < 1:
             raise ValueError("restarts must be >= 1")
         reference = None if rank_on is None else self._fp64_forces(rank_on)
